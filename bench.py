@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Throughput of the full hot path on one GB300: all 13 simplex relations plus
+critical-point classification, in Mtets/s.
+
+A step = one pass of the path over one mesh: tg_mesh_create (row sort,
+validation, VT) + tg_extract(all 13 relations) + tg_critical_points, then the
+mesh is destroyed.  The workload is the irregular single mesh: a 64^3 Kuhn
+grid with a seeded 20% of cubes centre-coned (1,887,438 tets, 327,054
+vertices), vertex ids permuted, float32 field = 32 Gaussians + N(0, 1e-3).
+
+  value  device-resident inputs (TV and field already in HBM), device outputs;
+         CUDA events on the launching stream around each step; L2 flushed
+         (a 512 MB write) before every step, outside the timed window.
+  e2e    the same steps through the C ABI with HOST buffers: pinned TV and
+         field copied in, and every relation plus the classes copied back to
+         pinned host memory, all inside the timed window.
+
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU
+(the path does not shard within a mesh); value = tets of all ranks / max time.
+
+--impl reference times the reference's CPU path (the C restatement of it in
+oracle/, the only build that exists on the GPU host) on the host cores: one
+process per core, each step a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mtets/s (13 relations + crit. points), batched vs per-mesh on 1 GB300; p99 ms"
+UNIT = "Mtets/s"
+WORKLOAD = "kuhn64_coned20_irregular"
+ROOFLINE_KERNEL = "k_star_b"
+# CPU sample for the baseline legs: cells [0, SAMPLE_CELLS) of the same mesh
+# (a valid mesh itself), run through the oracle.
+SAMPLE_CELLS = 262144
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, val in zip(names, parts[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes
+# ---------------------------------------------------------------------------
+def output_bytes(counts: dict, totals: dict) -> int:
+    """Compulsory bytes of the whole path: TV read once (16 B/tet), field read
+    once (4 B/vertex), every output written once (int32 entries, int64 CSR
+    offsets), classes written once (12 B/vertex)."""
+    V, E, F, T = counts["V"], counts["E"], counts["F"], counts["T"]
+    b = 16 * T + 4 * V + 12 * V
+    b += 4 * (6 * T + 2 * E + 4 * T + 3 * F + 3 * F + 2 * F)          # TE EV TF FV FE FT
+    for name, rows in (("ET", E), ("EF", E), ("VT", V), ("TT", T), ("FF", F), ("EE", E),
+                       ("VV", V)):
+        b += 8 * (rows + 1) + 4 * totals[name]
+    return b
+
+
+def kernel_bytes(name: str, c: dict, tot: dict) -> int:
+    """One-touch bytes of one kernel's inputs and outputs (each array read or
+    written once), per launch."""
+    V, E, F, T = c["V"], c["E"], c["F"], c["T"]
+    if name == "k_star_b":
+        reads = 16 * T + 16 * T + 8 * (V + 1) * 2 + 4 * 2 * E + 8 * 2 * E + (10 * T) // 8 \
+            + 4 * (10 * T) // 32
+        writes = 4 * 2 * E + 8 * E + 24 * T + 16 * T + 12 * F + 8 * F + 12 * E + 4 * F + 4 * T
+        return reads + writes
+    if name == "k_star_a":
+        return 16 * T + 16 * T + 8 * (V + 1) + 12 * 2 * E + 4 * V + (10 * T) // 8
+    if name == "k_ee_fill":
+        return 8 * E + 4 * 2 * E + 8 * (E + 1) + 8 * (V + 1) + 4 * tot["EE"]
+    if name == "k_star_c":
+        return 16 * T + 16 * T + 8 * (V + 1) + 16 * 2 * E + 4 * 2 * E + 8 * (E + 1) * 2 \
+            + 4 * tot["ET"] + 4 * tot["EF"]
+    raise KeyError(name)
+
+
+def traffic_from_profiles(kernel: str, workload: str, scale: float):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/*.md, a
+    line 'dram_bytes_per_launch: N' and 'cells: T'), scaled to this run."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    vals = {}
+    with open(p) as f:
+        for line in f:
+            if ":" in line and line.strip().startswith(("dram_bytes_per_launch", "cells")):
+                k, v = line.split(":", 1)
+                try:
+                    vals[k.strip()] = float(v.strip().split()[0].replace(",", ""))
+                except ValueError:
+                    pass
+    if "dram_bytes_per_launch" not in vals:
+        return None
+    b = vals["dram_bytes_per_launch"]
+    if "cells" in vals and vals["cells"] > 0:
+        b *= scale / vals["cells"]
+    return int(b)
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle = the reference CPU path restated in C)
+# ---------------------------------------------------------------------------
+def _cpu_sample_worker(args):
+    tv, n_verts, field, steps = args
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    o = Oracle()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        tvs = o.canonicalize(tv, n_verts)
+        o.extract(tvs, n_verts)
+        o.critical_points(tvs, n_verts, field)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def cpu_sample(mesh):
+    tv = np.ascontiguousarray(mesh.tv[:SAMPLE_CELLS])
+    return tv, mesh.n_verts, mesh.field
+
+
+def cpu_baseline(mesh) -> dict:
+    from oracle import oracle as O
+    O.build()
+    tv, nv, field = cpu_sample(mesh)
+    times = _cpu_sample_worker((tv, nv, field, 2))
+    t = min(times)
+    return {"value": round(tv.shape[0] / t / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"cells [0, {tv.shape[0]}) of the {WORKLOAD} mesh, all 13 relations + "
+                      f"critical points, single thread, best of 2 ({t:.2f} s)"}
+
+
+def run_reference(args):
+    rank, _, world = env_rank()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from tetragpu_gb300 import meshgen
+    O.build()
+    mesh = meshgen.workload_irregular()
+    tv, nv, field = cpu_sample(mesh)
+    cores = os.cpu_count() or 1
+    # warm-up + timed steps in every worker process, all cores busy at once
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        per = pool.map(_cpu_sample_worker, [(tv, nv, field, args.warmup + args.steps)] * cores)
+    wall = time.perf_counter() - t0
+    timed = [sum(t[args.warmup:]) for t in per]
+    tmax = max(timed)
+    value = cores * args.steps * tv.shape[0] / tmax / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * tmax / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells_per_step": int(tv.shape[0]),
+                   "note": "the reference CPU path (serial) restated in C; one process per core"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"cells [0, {tv.shape[0]}) of the {WORKLOAD} mesh per step, "
+                                   f"{cores} processes in parallel, wall {wall:.1f} s"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tetragpu", choices=["tetragpu", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    rank, local_rank, world = env_rank()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    import tetragpu_gb300 as tg
+    from tetragpu_gb300 import _build, meshgen
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    tg.load()
+
+    mesh = meshgen.workload_irregular()
+    T, V = mesh.n_cells, mesh.n_verts
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    d_tv = torch.from_numpy(mesh.tv).to(f"cuda:{local_rank}")
+    d_field = torch.from_numpy(mesh.field).to(f"cuda:{local_rank}")
+    d_classes = torch.empty(3 * V, dtype=torch.int32, device=f"cuda:{local_rank}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local_rank}")
+    torch.cuda.synchronize()
+
+    def step():
+        with tg.Mesh(d_tv.data_ptr(), V, n_cells=T, on_device=True, stream=s) as g:
+            g.extract(tg.ALL_RELATIONS, stream=s)
+            g.critical_points(d_field.data_ptr(), on_device=True, out_ptr=d_classes.data_ptr(),
+                              stream=s)
+            info = {"counts": g.counts()}
+            for n in ("ET", "EF", "VT", "TT", "FF", "EE", "VV"):
+                info[n] = g.device_relation(n)["n_entries"]
+        return info
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            info = step()
+    torch.cuda.synchronize()
+    Vc, E, F, Tc = info["counts"]
+    counts = {"V": Vc, "E": E, "F": F, "T": Tc}
+    totals = {n: info[n] for n in ("ET", "EF", "VT", "TT", "FF", "EE", "VV")}
+
+    # ---- timed region: device-resident inputs ----
+    clocks = Clocks(local_rank)
+    tg.profile_kernel(ROOFLINE_KERNEL)
+    tg.profile_read(reset=True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = tg.kernel_launch_count()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)          # evict L2 (outside the timed window)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = tg.kernel_launch_count() - launches0
+    clk = clocks.stop()
+    kern_ms, kern_n = tg.profile_read(reset=True)
+    tg.profile_kernel(None)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(ms) / 1e3
+    t_max = total_s
+    if world > 1:
+        t = torch.tensor([total_s], device=f"cuda:{local_rank}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    value = world * args.steps * T / t_max / 1e6
+
+    # ---- e2e: host buffers through the C ABI ----
+    pin_tv = torch.from_numpy(mesh.tv).pin_memory()
+    pin_field = torch.from_numpy(mesh.field).pin_memory()
+    names = tg.RELATIONS[1:]
+    host = {}
+    for n in names:
+        host[n] = (torch.empty(totals.get(n, 0) if n in totals else 0, dtype=torch.int32).pin_memory())
+    fixed_rows = {"TE": (Tc, 6), "EV": (E, 2), "TF": (Tc, 4), "FV": (F, 3), "FE": (F, 3),
+                  "FT": (F, 2)}
+    csr_rows = {"ET": E, "EF": E, "VT": Vc, "TT": Tc, "FF": F, "EE": E, "VV": Vc}
+    h_ent = {n: torch.empty(r * w, dtype=torch.int32).pin_memory() for n, (r, w) in fixed_rows.items()}
+    h_ent.update({n: torch.empty(totals[n], dtype=torch.int32).pin_memory() for n in csr_rows})
+    h_off = {n: torch.empty(r + 1, dtype=torch.int64).pin_memory() for n, r in csr_rows.items()}
+    h_cls = np.empty((V, 3), dtype=np.uint32)
+    h2d = pin_tv.numel() * 4 + pin_field.numel() * 4
+    d2h = sum(x.numel() * 4 for x in h_ent.values()) + sum(x.numel() * 8 for x in h_off.values()) \
+        + h_cls.nbytes
+    lib = tg.load()
+
+    def e2e_step():
+        with tg.Mesh(pin_tv.numpy(), V, stream=s) as g:
+            g.extract(tg.ALL_RELATIONS, stream=s)
+            tg._lib.check(lib.tg_critical_points(g._h, pin_field.data_ptr(), tg.FIELD_F32, 0,
+                                                 h_cls.ctypes.data, 0, s))
+            for n in names:
+                tg._lib.check(lib.tg_copy_relation(
+                    g._h, tg.REL[n], h_off[n].data_ptr() if n in h_off else None,
+                    h_ent[n].data_ptr() if h_ent[n].numel() else None, s))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local_rank}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.e2e_steps * T / e2e_s / 1e6
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        kb = kernel_bytes(ROOFLINE_KERNEL, counts, totals)
+        per_launch_s = (kern_ms / 1e3) / max(kern_n, 1)
+        achieved = kb / per_launch_s / 1e9 if kern_n else None
+        traffic = traffic_from_profiles(ROOFLINE_KERNEL, WORKLOAD, T)
+        alg = output_bytes(counts, totals)
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": round(1e3 * t_max / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": T, "vertices": V, "edges": E, "faces": F,
+                       "relations": "all 13 + critical points", "parallelism": f"replicas{world}",
+                       "l2": "flushed before every step (512 MB write)",
+                       "path_bytes_per_step": alg,
+                       "path_gbs_of_measured_peak": round(alg / (t_max / args.steps) / 1e9 / peak, 4)},
+            "gpu_launches": int(launches),
+            "wall_s": round(wall, 3),
+            "clocks": clk,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
+            "roofline": {"bound": "hbm", "kernel": ROOFLINE_KERNEL,
+                         "achieved": round(achieved, 1) if achieved else None, "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": kb,
+                         "launch_ms": round(per_launch_s * 1e3, 4), "launches": kern_n,
+                         "traffic": traffic},
+        }
+        if not args.no_cpu_baseline and world >= 1:
+            line["cpu_baseline"] = cpu_baseline(mesh)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

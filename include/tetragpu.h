@@ -1,0 +1,173 @@
+/*
+ * tetragpu.h -- C ABI of the GB300-native (sm_103a) relation-extraction and
+ * critical-point library, libtetragpu.so.
+ *
+ * This is the drop-in boundary for TetraGPU's hot path.  It replaces the
+ * reference's C++ entry points in include/cuda_extraction.h (tlranda/TetraGPU)
+ * and the critPoints kernel launch in src/alg/critPoints.cu; each function
+ * below names the reference interface it stands in for.  Plain C: pointers,
+ * sizes and integer status codes only.  A CUDA stream is passed as void* (a
+ * cudaStream_t cast); NULL means the legacy default stream.
+ *
+ * Data model (the reference's TV-in / CSR-out layout, kept as is):
+ *   - TV is int32 [n_cells x 4].  The library sorts every row ascending
+ *     before numbering (the reference CPU face numbering is only consistent
+ *     on sorted rows, src/cpu_extraction.cpp:136-153); TE and TF columns refer
+ *     to the sorted row.
+ *   - Edge ids and face ids are the reference CPU ids: the rank of each
+ *     edge's / face's first occurrence when cells are scanned in order,
+ *     edges of a cell in pair order (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
+ *     (src/cpu_extraction.cpp:28-62), faces visited with skip (the omitted
+ *     slot) = 3,2,1,0, which is TF column order 0..3 (column = 3 - skip,
+ *     src/cpu_extraction.cpp:122-174).
+ *   - Fixed-width relations (TE 6, EV 2, TF 4, FV 3, FE 3, FT 2) are dense
+ *     row-major int32.  FT pads a boundary face's missing cell with -1.
+ *   - Variable-width relations (ET, EF, VT, TT, FF, EE, VV) are CSR: int64
+ *     offsets [n_rows + 1] and int32 entries, each row sorted ascending.
+ *     Exact size: no padding, no duplicates.
+ *   - Relations live in device memory owned by the mesh handle until
+ *     tg_mesh_destroy (the reference returned raw device pointers the caller
+ *     had to cudaFree, src/cuda_extraction.cu:3-22).
+ *
+ * Errors are status codes (the reference exit()s, include/cuda_safety.h:19-27);
+ * tg_last_error_string() describes the last failure on the calling thread.
+ * Handles are independent: one mesh per thread needs no locking (the
+ * reference keeps its device inputs in file-scope globals,
+ * src/cuda_extraction.cu:62,82-84,158-160).
+ */
+#ifndef TETRAGPU_H
+#define TETRAGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TG_OK = 0,
+    TG_ERR_INVALID_ARGUMENT = 1,
+    TG_ERR_INVALID_MESH = 2,    /* id out of range, repeated vertex, face in >2 cells */
+    TG_ERR_CUDA = 3,
+    TG_ERR_OUT_OF_MEMORY = 4,
+    TG_ERR_UNSUPPORTED = 5,     /* a limit of this build was exceeded (message says which) */
+    TG_ERR_NOT_COMPUTED = 6,    /* relation not extracted yet */
+    TG_ERR_TIMEOUT = 7
+} tg_status;
+
+/* Relation bits: the reference's arg_flags bit positions
+ * (include/datatypes.h.in:164-197, set by --build_XX in src/argparse.cu:82-94).
+ * Bit 0 (validate) is accepted and ignored: validation is the test suite's
+ * job, against the CPU oracle. */
+#define TG_VALIDATE (1u << 0)
+#define TG_TE (1u << 1)
+#define TG_EV (1u << 2)
+#define TG_ET (1u << 3)
+#define TG_TF (1u << 4)
+#define TG_FV (1u << 5)
+#define TG_FE (1u << 6)
+#define TG_FT (1u << 7)
+#define TG_EF (1u << 8)
+#define TG_VT (1u << 9)
+#define TG_TT (1u << 10)
+#define TG_FF (1u << 11)
+#define TG_EE (1u << 12)
+#define TG_VV (1u << 13)
+#define TG_ALL_RELATIONS 0x3FFEu
+
+/* relation index = bit position */
+enum {
+    TG_REL_TE = 1, TG_REL_EV = 2, TG_REL_ET = 3, TG_REL_TF = 4, TG_REL_FV = 5,
+    TG_REL_FE = 6, TG_REL_FT = 7, TG_REL_EF = 8, TG_REL_VT = 9, TG_REL_TT = 10,
+    TG_REL_FF = 11, TG_REL_EE = 12, TG_REL_VV = 13
+};
+
+/* tg_extract options */
+#define TG_OPT_TT_VERTEX_SHARING 0x1u /* TT = cells sharing >= 1 vertex (default: sharing a face) */
+
+/* critical-point field types */
+#define TG_FIELD_F32 0
+#define TG_FIELD_F64 1
+
+typedef struct tg_mesh tg_mesh;
+
+/* Library version string. */
+const char *tg_version(void);
+
+/* Description of the last error on this thread ("" if none). */
+const char *tg_last_error_string(void);
+
+/* Create a mesh from TV (int32 [n_cells x 4]) in host memory (tv_on_device =
+ * 0) or device memory (1) of the current device.  Sorts rows, validates ids
+ * and builds VT.  Replaces make_TV_for_GPU (src/cuda_extraction.cu:62-80),
+ * without its single-use global and its int/vtkIdType size mix-up (:71). */
+tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts,
+                         int tv_on_device, void *stream, tg_mesh **out);
+
+tg_status tg_mesh_destroy(tg_mesh *mesh);
+
+/* Extract every relation whose bit is set (plus what they depend on) and keep
+ * them resident.  Replaces the make_X_GPU_return family
+ * (include/cuda_extraction.h:27-138) and the CPU id minting they depended on
+ * (make_TE_and_VE / make_TF_and_VF, src/cpu_extraction.cpp:28-174).
+ * Returns after the work is enqueued and the sizes are known (it
+ * synchronises the stream a few times to size the outputs). */
+tg_status tg_extract(tg_mesh *mesh, uint32_t relation_mask, uint32_t options,
+                     void *stream);
+
+/* Counts: vertices, edges (-1 until edges are numbered), faces (-1 until
+ * faces are numbered), cells. */
+tg_status tg_mesh_counts(const tg_mesh *mesh, int64_t *n_verts, int64_t *n_edges,
+                         int64_t *n_faces, int64_t *n_cells);
+
+/* Device pointers of an extracted relation.  Fixed-width relations return
+ * offsets == NULL and *row_width = width; CSR relations *row_width = 0.
+ * Pointers stay valid until the mesh is destroyed or the relation is
+ * re-extracted with different options. */
+tg_status tg_get_relation(const tg_mesh *mesh, int relation, const int64_t **offsets,
+                          const int32_t **entries, int64_t *n_rows, int64_t *n_entries,
+                          int32_t *row_width);
+
+/* Copy a relation to host buffers (offsets may be NULL for fixed width, or
+ * to skip them).  Synchronous with respect to the host. */
+tg_status tg_copy_relation(const tg_mesh *mesh, int relation, int64_t *offsets_host,
+                           int32_t *entries_host, void *stream);
+
+/* Device pointer of the canonical (row-sorted) TV, int32 [n_cells x 4]. */
+tg_status tg_get_tv(const tg_mesh *mesh, const int32_t **tv_sorted);
+
+/* Classify every vertex of a scalar field (float32 or float64, host or
+ * device, n_verts values).  Writes uint32 [n_verts x 3] in the reference
+ * layout of critPoints (src/alg/critPoints.cu:275-331): [3v] lower-link
+ * components, [3v+1] upper-link components, [3v+2] class code with the
+ * reference's numeric values: 1 minimum, 2 maximum, 3 regular, 4 saddle.
+ * A neighbour u of v is lower when f[u] < f[v], or f[u] == f[v] and u < v;
+ * two neighbours are linked when the mesh has an edge between them (the
+ * reference's VV test, critPoints.cu:172-202).  classes_out is host memory
+ * (out_on_device = 0, synchronous) or device memory (1, stream-ordered).
+ * Extracts VV if needed.  The field-independent part (the link adjacency) is
+ * cached on the mesh, so a second field costs only the classification. */
+tg_status tg_critical_points(tg_mesh *mesh, const void *field, int field_type,
+                             int field_on_device, uint32_t *classes_out,
+                             int out_on_device, void *stream);
+
+/* Bytes of device memory the mesh currently holds. */
+int64_t tg_mesh_device_bytes(const tg_mesh *mesh);
+
+/* Number of kernel launches this library has issued in this process. */
+int64_t tg_kernel_launch_count(void);
+
+/* Time every launch of one kernel (by name, e.g. "k_star_b") with CUDA
+ * events recorded on the stream it is launched on; NULL or "" turns timing
+ * off.  For measurement tools; the reference's analogue is its Timer class
+ * (src/metrics.cpp).  Not thread-safe against concurrent extractions. */
+tg_status tg_profile_kernel(const char *name);
+
+/* Sum of the timed launches' durations (waits for them), their number, and
+ * optionally forget them. */
+tg_status tg_profile_read(double *total_ms, int64_t *launches, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,126 @@
+"""CUDA path (through the C ABI) against the CPU oracle: bit-exact on every
+relation and on the critical-point classes."""
+import numpy as np
+import pytest
+
+from helpers import RELS, assert_relations_equal, gpu_extract_all
+from tetragpu_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_mesh(tg, oracle, m, options=0):
+    tvs = oracle.canonicalize(m.tv, m.n_verts)
+    ref = oracle.extract(tvs, m.n_verts, options=options)
+    got = gpu_extract_all(tg, m.tv, m.n_verts, options=options)
+    assert got["counts"] == ref["counts"]
+    assert_relations_equal(got, ref)
+    return ref
+
+
+@pytest.mark.parametrize("name", ["two_tets", "kuhn_cube", "coned_cube"])
+def test_tiny_known_answers(gpu_lib, oracle, name):
+    m, counts = meshgen.tiny_meshes()[name]
+    ref = _check_mesh(gpu_lib, oracle, m)
+    assert ref["counts"] == counts
+
+
+def test_small_kuhn16(gpu_lib, oracle):
+    _check_mesh(gpu_lib, oracle, meshgen.workload_small())
+
+
+@pytest.mark.parametrize("seed,frac", [(3, 0.0), (4, 0.2), (5, 1.0)])
+def test_coned_grids(gpu_lib, oracle, seed, frac):
+    _check_mesh(gpu_lib, oracle, meshgen.kuhn_mesh((7, 5, 9), frac, seed=seed))
+
+
+def test_tt_vertex_sharing(gpu_lib, oracle):
+    m = meshgen.kuhn_mesh(5, 0.3, seed=9)
+    tvs = oracle.canonicalize(m.tv, m.n_verts)
+    ref = oracle.extract(tvs, m.n_verts, mask=1 << 10, options=1)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        g.extract(["TT"], options=gpu_lib.OPT_TT_VERTEX_SHARING)
+        got = g.relation("TT")
+    assert np.array_equal(got[0], ref["TT"][0]) and np.array_equal(got[1], ref["TT"][1])
+
+
+def test_unsorted_rows_and_isolated_vertices(gpu_lib, oracle):
+    # slots shuffled, plus 5 vertex ids that no cell uses
+    m = meshgen.kuhn_mesh(3, 0.5, seed=21)
+    m.n_verts += 5
+    _check_mesh(gpu_lib, oracle, m)
+
+
+def test_empty_mesh(gpu_lib):
+    with gpu_lib.Mesh(np.zeros((0, 4), np.int32), 7) as g:
+        g.extract(gpu_lib.ALL_RELATIONS)
+        assert g.counts() == (7, 0, 0, 0)
+        off, ent = g.relation("VV")
+        assert np.array_equal(off, np.zeros(8, np.int64)) and ent.size == 0
+        cp = g.critical_points(np.arange(7, dtype=np.float32))
+        assert (cp[:, 2] == 4).all()
+
+
+@pytest.mark.parametrize("bad,code", [([[0, 1, 2, 9]], 2), ([[0, 1, 1, 2]], 2), ([[0, -1, 2, 3]], 2)])
+def test_invalid_meshes_rejected(gpu_lib, bad, code):
+    with pytest.raises(gpu_lib.TetraGPUError) as ei:
+        gpu_lib.Mesh(np.array(bad, np.int32), 4)
+    assert ei.value.code == code
+
+
+def test_nonmanifold_face_rejected(gpu_lib):
+    tv = np.array([[0, 1, 2, 3], [0, 1, 2, 4], [0, 1, 2, 5]], np.int32)
+    with gpu_lib.Mesh(tv, 6) as g:
+        with pytest.raises(gpu_lib.TetraGPUError) as ei:
+            g.extract(["TF"])
+        assert ei.value.code == 2
+
+
+def test_nonmanifold_vertex_star(gpu_lib, oracle):
+    # two tets touching at one vertex: 6 neighbours around a 2-cell star,
+    # beyond the manifold bound (cells + 2); the wide summary takes over
+    tv = np.array([[0, 1, 2, 3], [0, 4, 5, 6]], np.int32)
+    ref = oracle.extract(tv, 7)
+    got = gpu_extract_all(gpu_lib, tv, 7)
+    assert_relations_equal(got, ref)
+
+
+def test_critical_points_small(gpu_lib, oracle):
+    m = meshgen.workload_small()
+    tvs = oracle.canonicalize(m.tv, m.n_verts)
+    ref = oracle.critical_points(tvs, m.n_verts, m.field)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        got = g.critical_points(m.field)
+        # second field on the same mesh reuses the cached link adjacency
+        f2 = meshgen.sine_field(m.coords, seed=3)
+        got2 = g.critical_points(f2.astype(np.float64))
+    assert np.array_equal(got, ref)
+    assert np.array_equal(got2, oracle.critical_points(tvs, m.n_verts, f2.astype(np.float64)))
+
+
+def test_critical_points_ties_broken_by_id(gpu_lib, oracle):
+    m = meshgen.kuhn_mesh(4, 0.25, seed=2)
+    field = np.round(meshgen.gaussian_mixture_field(m.coords, n_gauss=4, seed=5) * 4) / 4
+    tvs = oracle.canonicalize(m.tv, m.n_verts)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        got = g.critical_points(field.astype(np.float32))
+    assert np.array_equal(got, oracle.critical_points(tvs, m.n_verts, field.astype(np.float32)))
+
+
+def test_irregular_full(gpu_lib, oracle):
+    """The 64^3, 20%-coned workload: all 13 relations and critical points."""
+    m = meshgen.workload_irregular()
+    tvs = oracle.canonicalize(m.tv, m.n_verts)
+    ref = oracle.extract(tvs, m.n_verts)
+    ref_cp = oracle.critical_points(tvs, m.n_verts, m.field)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        g.extract(gpu_lib.ALL_RELATIONS)
+        assert g.counts() == ref["counts"]
+        for n in RELS:
+            got = g.relation(n)
+            want = ref[n]
+            if isinstance(want, tuple):
+                assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), n
+            else:
+                assert np.array_equal(got, want), n
+        assert np.array_equal(g.critical_points(m.field), ref_cp)

@@ -1,0 +1,216 @@
+"""ctypes binding of libtetragpu.so (the C ABI in include/tetragpu.h).
+
+There is no CPU fallback: if the library is missing or fails to load, every
+call raises.  Build it with ``tetragpu_gb300._build.build()`` (nvcc,
+sm_103a).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+RELATIONS = ["validate", "TE", "EV", "ET", "TF", "FV", "FE", "FT", "EF", "VT",
+             "TT", "FF", "EE", "VV"]
+REL = {name: i for i, name in enumerate(RELATIONS)}
+ALL_RELATIONS = 0x3FFE
+OPT_TT_VERTEX_SHARING = 0x1
+FIELD_F32, FIELD_F64 = 0, 1
+
+STATUS = {0: "TG_OK", 1: "TG_ERR_INVALID_ARGUMENT", 2: "TG_ERR_INVALID_MESH", 3: "TG_ERR_CUDA",
+          4: "TG_ERR_OUT_OF_MEMORY", 5: "TG_ERR_UNSUPPORTED", 6: "TG_ERR_NOT_COMPUTED",
+          7: "TG_ERR_TIMEOUT"}
+
+
+class TetraGPUError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def mask_of(names) -> int:
+    m = 0
+    for n in names:
+        m |= 1 << REL[n]
+    return m
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Load libtetragpu.so from the package directory (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with tetragpu_gb300._build.build() "
+                           "(there is no CPU fallback)")
+    lib = C.CDLL(path)
+    vp, i64, i32, u32 = C.c_void_p, C.c_int64, C.c_int32, C.c_uint32
+    P = C.POINTER
+    sig = {
+        "tg_version": (C.c_char_p, []),
+        "tg_last_error_string": (C.c_char_p, []),
+        "tg_mesh_create": (C.c_int, [vp, i64, i64, C.c_int, vp, P(vp)]),
+        "tg_mesh_destroy": (C.c_int, [vp]),
+        "tg_extract": (C.c_int, [vp, u32, u32, vp]),
+        "tg_mesh_counts": (C.c_int, [vp, P(i64), P(i64), P(i64), P(i64)]),
+        "tg_get_relation": (C.c_int, [vp, C.c_int, P(vp), P(vp), P(i64), P(i64), P(i32)]),
+        "tg_copy_relation": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "tg_get_tv": (C.c_int, [vp, P(vp)]),
+        "tg_critical_points": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]),
+        "tg_mesh_device_bytes": (i64, [vp]),
+        "tg_kernel_launch_count": (i64, []),
+        "tg_profile_kernel": (C.c_int, [C.c_char_p]),
+        "tg_profile_read": (C.c_int, [P(C.c_double), P(i64), C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != 0:
+        raise TetraGPUError(rc, load().tg_last_error_string().decode())
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class Mesh:
+    """A mesh resident on the current CUDA device.
+
+    ``tv`` is an int32 [n_cells, 4] numpy array (host) or a device pointer
+    (int) with ``on_device=True``.
+    """
+
+    def __init__(self, tv, n_verts: int, n_cells: int | None = None, on_device: bool = False,
+                 stream=None):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        if on_device:
+            ptr = int(tv)
+            assert n_cells is not None, "n_cells is required for a device pointer"
+            keep = None
+        else:
+            keep = np.ascontiguousarray(tv, dtype=np.int32).reshape(-1, 4)
+            ptr = keep.ctypes.data if keep.size else None
+            n_cells = keep.shape[0]
+        self.n_cells = int(n_cells)
+        self.n_verts = int(n_verts)
+        check(lib.tg_mesh_create(ptr, self.n_cells, self.n_verts, int(bool(on_device)),
+                                 _stream(stream), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            self._lib.tg_mesh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def extract(self, relations=ALL_RELATIONS, options: int = 0, stream=None):
+        mask = relations if isinstance(relations, int) else mask_of(relations)
+        check(self._lib.tg_extract(self._h, mask, options, _stream(stream)))
+        return self
+
+    def counts(self) -> tuple:
+        v, e, f, t = (C.c_int64() for _ in range(4))
+        check(self._lib.tg_mesh_counts(self._h, C.byref(v), C.byref(e), C.byref(f), C.byref(t)))
+        return v.value, e.value, f.value, t.value
+
+    def device_relation(self, name: str) -> dict:
+        off, ent = C.c_void_p(), C.c_void_p()
+        rows, n, width = C.c_int64(), C.c_int64(), C.c_int32()
+        check(self._lib.tg_get_relation(self._h, REL[name], C.byref(off), C.byref(ent),
+                                        C.byref(rows), C.byref(n), C.byref(width)))
+        return {"offsets": off.value, "entries": ent.value, "rows": rows.value,
+                "n_entries": n.value, "width": width.value}
+
+    def relation(self, name: str, stream=None):
+        """Host copy: [rows, width] array, or (offsets int64, entries int32)."""
+        d = self.device_relation(name)
+        ent = np.empty(d["n_entries"], dtype=np.int32)
+        if d["width"] > 0:
+            check(self._lib.tg_copy_relation(self._h, REL[name], None,
+                                             ent.ctypes.data if ent.size else None, _stream(stream)))
+            return ent.reshape(d["rows"], d["width"])
+        off = np.empty(d["rows"] + 1, dtype=np.int64)
+        check(self._lib.tg_copy_relation(self._h, REL[name], off.ctypes.data,
+                                         ent.ctypes.data if ent.size else None, _stream(stream)))
+        return off, ent
+
+    def tv_sorted_ptr(self) -> int:
+        p = C.c_void_p()
+        check(self._lib.tg_get_tv(self._h, C.byref(p)))
+        return p.value
+
+    def critical_points(self, field, on_device: bool = False, out_ptr: int | None = None,
+                        field_type: int | None = None, stream=None):
+        """uint32 [V, 3] (lower comps, upper comps, class code); with
+        ``out_ptr`` the result goes to device memory and None is returned."""
+        if on_device:
+            fptr = int(field)
+            ftype = FIELD_F32 if field_type is None else field_type
+        else:
+            arr = np.ascontiguousarray(field)
+            if arr.dtype == np.float64:
+                ftype = FIELD_F64
+            else:
+                arr = arr.astype(np.float32, copy=False)
+                ftype = FIELD_F32
+            fptr = arr.ctypes.data
+        if out_ptr is not None:
+            check(self._lib.tg_critical_points(self._h, fptr, ftype, int(bool(on_device)),
+                                               int(out_ptr), 1, _stream(stream)))
+            return None
+        out = np.empty((self.n_verts, 3), dtype=np.uint32)
+        check(self._lib.tg_critical_points(self._h, fptr, ftype, int(bool(on_device)),
+                                           out.ctypes.data, 0, _stream(stream)))
+        return out
+
+    def device_bytes(self) -> int:
+        return int(self._lib.tg_mesh_device_bytes(self._h))
+
+
+def kernel_launch_count() -> int:
+    return int(load().tg_kernel_launch_count())
+
+
+def profile_kernel(name: str | None):
+    """Time every launch of the named kernel with CUDA events."""
+    check(load().tg_profile_kernel(name.encode() if name else None))
+
+
+def profile_read(reset: bool = True) -> tuple:
+    """(total milliseconds, number of timed launches) since the last reset."""
+    ms, n = C.c_double(), C.c_int64()
+    check(load().tg_profile_read(C.byref(ms), C.byref(n), int(reset)))
+    return ms.value, n.value
+
+
+def version() -> str:
+    return load().tg_version().decode()

@@ -1,0 +1,737 @@
+// tg_api.cu -- host orchestration of the relation pipeline behind the C ABI
+// declared in include/tetragpu.h.
+//
+// One tg_mesh owns its device buffers.  Memory comes from the device's
+// stream-ordered pool (cudaMallocAsync) with an unlimited release threshold,
+// so repeated extractions reuse blocks instead of returning them to the
+// driver.  tg_extract synchronises the stream at two points, to learn the
+// edge/face/neighbour counts and then the CSR totals that size the outputs;
+// everything between those points is asynchronous on the caller's stream.
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tetragpu.h"
+#include "tg_internal.h"
+
+namespace tg {
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Optional timing of one named kernel with CUDA events on its own stream
+// (tg_profile_kernel / tg_profile_read).  Off unless a name is set.
+namespace {
+std::mutex g_prof_mu;
+std::string g_prof_name;
+std::atomic<bool> g_prof_on{false};
+struct EvPair {
+    cudaEvent_t a, b;
+};
+std::vector<EvPair> g_prof_events;
+std::vector<cudaEvent_t> g_prof_pool;
+cudaEvent_t g_prof_open = nullptr;
+
+cudaEvent_t prof_event()
+{
+    if (!g_prof_pool.empty()) {
+        cudaEvent_t e = g_prof_pool.back();
+        g_prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+void prof_begin(const char *name, cudaStream_t s)
+{
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (g_prof_name != name) return;
+    g_prof_open = prof_event();
+    cudaEventRecord(g_prof_open, s);
+}
+
+void prof_end(const char *name, cudaStream_t s)
+{
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (g_prof_name != name || !g_prof_open) return;
+    cudaEvent_t b = prof_event();
+    cudaEventRecord(b, s);
+    g_prof_events.push_back({g_prof_open, b});
+    g_prof_open = nullptr;
+}
+}  // namespace tg
+
+using namespace tg;
+
+namespace {
+
+thread_local std::string g_err;
+
+tg_status fail(tg_status code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+tg_status cuda_fail(cudaError_t e, const char *what, int line)
+{
+    (void)cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? TG_ERR_OUT_OF_MEMORY : TG_ERR_CUDA,
+                "%s (%s) at tg_api.cu:%d: %s", cudaGetErrorName(e), cudaGetErrorString(e), line,
+                what);
+}
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call, __LINE__);   \
+    } while (0)
+
+#define TRY(expr)                                   \
+    do {                                            \
+        tg_status _s = (expr);                      \
+        if (_s != TG_OK) return _s;                 \
+    } while (0)
+
+constexpr int64_t kMaxCells = 357913941LL;  // 6 * cells must fit in 31 bits
+
+std::mutex g_pool_mu;
+bool g_pool_ready[64];
+
+void setup_pool(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (dev < 0 || dev >= 64 || g_pool_ready[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    (void)cudaGetLastError();
+    g_pool_ready[dev] = true;
+}
+
+struct Rel {
+    int64_t rows = 0, entries = 0;
+    int width = 0;
+    int64_t *off = nullptr;
+    int32_t *ent = nullptr;
+    bool ready = false;
+    uint32_t opts = 0;
+};
+
+const int kWidth[14] = {0, 6, 2, 0, 4, 3, 3, 2, 0, 0, 0, 0, 0, 0};
+const char *kName[14] = {"validate", "TE", "EV", "ET", "TF", "FV", "FE",
+                         "FT",       "EF", "VT", "TT", "FF", "EE", "VV"};
+
+// Scoped list of stream-ordered temporaries, freed when the stage ends.
+struct Temps {
+    cudaStream_t s;
+    void *p[32];
+    int n = 0;
+    explicit Temps(cudaStream_t st) : s(st) {}
+    ~Temps()
+    {
+        for (int i = 0; i < n; i++)
+            if (p[i]) cudaFreeAsync(p[i], s);
+    }
+    template <class T>
+    tg_status alloc(T **out, int64_t count, bool zero = false)
+    {
+        size_t b = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+        void *q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, b, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (temporary)", __LINE__);
+        if (zero) {
+            e = cudaMemsetAsync(q, 0, b, s);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync", __LINE__);
+        }
+        p[n++] = q;
+        *out = (T *)q;
+        return TG_OK;
+    }
+    // hand a temporary over to the caller (it is not freed here)
+    void keep(void *q)
+    {
+        for (int i = 0; i < n; i++)
+            if (p[i] == q) p[i] = nullptr;
+    }
+};
+
+template <class T>
+tg_status dalloc(T **out, int64_t count, cudaStream_t s)
+{
+    size_t b = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+    void *q = nullptr;
+    cudaError_t e = cudaMallocAsync(&q, b, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync", __LINE__);
+    *out = (T *)q;
+    return TG_OK;
+}
+
+}  // namespace
+
+struct tg_mesh {
+    int device = 0;
+    int64_t V = 0, T = 0, E = -1, F = -1;
+    int4 *tvs = nullptr;
+    Rel rel[14];
+    uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
+    DevStatus *st = nullptr;    // device
+    DevStatus *st_host = nullptr;
+    int64_t *sz_host = nullptr; // pinned slots for sizes read back at sync points
+};
+
+namespace {
+
+void free_rel(Rel &r)
+{
+    if (r.off) cudaFree(r.off);
+    if (r.ent) cudaFree(r.ent);
+    r = Rel();
+}
+
+tg_status reset_status(tg_mesh *m, cudaStream_t s)
+{
+    DevStatus init{};
+    init.flags = 0;
+    init.bad_cell = INT_MAX;
+    init.bad_vertex = INT_MAX;
+    CK(cudaStreamSynchronize(s));  // st_host may still be the source of an earlier copy
+    *m->st_host = init;
+    CK(cudaMemcpyAsync(m->st, m->st_host, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+
+// Read the status word plus up to 8 device scalars (int64 if `wide[i]`,
+// else int32) into m->sz_host, synchronously.
+tg_status sync_read(tg_mesh *m, cudaStream_t s, int n, const void *const *src, const bool *wide)
+{
+    CK(cudaMemcpyAsync(m->st_host, m->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    for (int i = 0; i < n; i++) {
+        m->sz_host[i] = 0;
+        CK(cudaMemcpyAsync(&m->sz_host[i], src[i], wide[i] ? 8 : 4, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; i++)
+        if (!wide[i]) m->sz_host[i] = (int64_t)(int32_t)m->sz_host[i];
+    return TG_OK;
+}
+
+tg_status check_flags(const tg_mesh *m, unsigned mask_ok = 0)
+{
+    const DevStatus &h = *m->st_host;
+    const unsigned f = h.flags & ~mask_ok;
+    if (!f) return TG_OK;
+    if (f & ST_BAD_ID)
+        return fail(TG_ERR_INVALID_MESH, "cell %d has a vertex id outside [0, %lld)", h.bad_cell,
+                    (long long)m->V);
+    if (f & ST_DUP_VERTEX)
+        return fail(TG_ERR_INVALID_MESH, "cell %d repeats a vertex", h.bad_cell);
+    if (f & ST_NONMANIFOLD_FACE)
+        return fail(TG_ERR_INVALID_MESH, "a face of cell %d lies in more than two cells",
+                    h.bad_cell);
+    if (f & ST_HEAVY_STAR)
+        return fail(TG_ERR_UNSUPPORTED,
+                    "vertex %d lies in more than %d cells (largest star this build handles)",
+                    h.bad_vertex, kMaxStar);
+    if (f & ST_HEAVY_DEG)
+        return fail(TG_ERR_UNSUPPORTED,
+                    "a vertex has %d neighbours (more than %d, the largest this build handles)",
+                    h.max_deg, kMaxDeg);
+    if (f & ST_HASH_FULL)
+        return fail(TG_ERR_UNSUPPORTED, "vertex %d: neighbour table overflow", h.bad_vertex);
+    if (f & ST_STAR_OVERFLOW)
+        return fail(TG_ERR_UNSUPPORTED, "vertex %d: neighbour summary overflow", h.bad_vertex);
+    return fail(TG_ERR_CUDA, "unexpected device status 0x%x", f);
+}
+
+inline uint32_t bit(int r) { return 1u << r; }
+
+tg_status set_fixed(tg_mesh *m, int r, int32_t *ent, int64_t rows)
+{
+    free_rel(m->rel[r]);
+    Rel &x = m->rel[r];
+    x.rows = rows;
+    x.width = kWidth[r];
+    x.entries = rows * kWidth[r];
+    x.ent = ent;
+    x.ready = true;
+    return TG_OK;
+}
+
+void set_csr(tg_mesh *m, int r, int64_t *off, int32_t *ent, int64_t rows, int64_t entries,
+             uint32_t opts = 0)
+{
+    free_rel(m->rel[r]);
+    Rel &x = m->rel[r];
+    x.rows = rows;
+    x.entries = entries;
+    x.width = 0;
+    x.off = off;
+    x.ent = ent;
+    x.ready = true;
+    x.opts = opts;
+}
+
+tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
+{
+    const int64_t V = m->V, T = m->T;
+    const bool tt_vertex = (opts & TG_OPT_TT_VERTEX_SHARING) != 0;
+    const bool want_tt_face = (mask & TG_TT) && !tt_vertex;
+    const uint32_t starb_rel = TG_TE | TG_EV | TG_ET | TG_TF | TG_FV | TG_FE | TG_FT | TG_EF |
+                               TG_FF | TG_EE;
+    const bool want_b = (mask & starb_rel) || want_tt_face;
+    const bool want_vv = want_b || (mask & TG_VV);
+    const int64_t *vt_off = m->rel[TG_REL_VT].off;
+    const int32_t *vt = m->rel[TG_REL_VT].ent;
+    Temps tmp(s);
+
+    if (want_vv) {
+        TRY(reset_status(m, s));
+        const int64_t nwe = (6 * T + 31) / 32, nwf = (4 * T + 31) / 32;
+        uint32_t *eflag, *fflag;
+        int32_t *epre, *fpre, *deg;
+        int64_t *vv_off;
+        TRY(tmp.alloc(&eflag, nwe));
+        TRY(tmp.alloc(&fflag, nwf));
+        TRY(tmp.alloc(&epre, nwe + 1));
+        TRY(tmp.alloc(&fpre, nwf + 1));
+        TRY(tmp.alloc(&deg, V));
+        TRY(dalloc(&vv_off, V + 1, s));
+        char *scratch;
+        const int64_t maxn = std::max(V, std::max(nwe, nwf));
+        TRY(tmp.alloc(&scratch, 3 * (int64_t)(scan_scratch_bytes(maxn) + 256)));
+
+        int32_t *sum_nb = nullptr;
+        uint64_t *sum_mask = nullptr;
+        uint64_t *vvmask = nullptr;
+        int wide = 0;
+        for (int attempt = 0; attempt < 2; attempt++) {
+            const int64_t cap = wide ? 3 * 4 * T : 4 * T + 2 * V;
+            Temps sum(s);
+            TRY(sum.alloc(&sum_nb, cap));
+            TRY(sum.alloc(&sum_mask, cap));
+            CK(cudaMemsetAsync(eflag, 0, nwe * 4, s));
+            CK(cudaMemsetAsync(fflag, 0, nwf * 4, s));
+            StarA a{vt_off, vt, m->tvs, V, deg, sum_nb, sum_mask, eflag, fflag, m->st, wide};
+            launch_star_a(a, s);
+            ScanJob jobs[3] = {{deg, vv_off, V, SCAN_COUNT_I32, 0},
+                               {eflag, epre, nwe, SCAN_POPC_U32, 0},
+                               {fflag, fpre, nwf, SCAN_POPC_U32, 0}};
+            scan_batch(jobs, 3, scratch, s);
+            const void *src[3] = {vv_off + V, epre + nwe, fpre + nwf};
+            const bool w8[3] = {true, false, false};
+            TRY(sync_read(m, s, 3, src, w8));
+            if ((m->st_host->flags & ST_STAR_OVERFLOW) && !wide &&
+                !(m->st_host->flags & ~ST_STAR_OVERFLOW)) {
+                // a non-manifold vertex: redo with the always-sufficient capacity
+                wide = 1;
+                TRY(reset_status(m, s));
+                continue;
+            }
+            if (m->st_host->flags) {
+                cudaFreeAsync(vv_off, s);
+                return check_flags(m);
+            }
+            const int64_t nvv = m->sz_host[0];
+            m->E = m->sz_host[1];
+            m->F = m->sz_host[2];
+            int32_t *vv;
+            TRY(dalloc(&vv, nvv, s));
+            TRY(tmp.alloc(&vvmask, nvv));
+            launch_vv_finalize(vt_off, sum_nb, sum_mask, vv_off, V, wide, vv, vvmask, s);
+            set_csr(m, TG_REL_VV, vv_off, vv, V, nvv);
+            if (m->cadj) {
+                cudaFreeAsync(m->cadj, s);
+                m->cadj = nullptr;
+            }
+            break;
+        }
+        if (want_b) {
+            const int64_t E = m->E, F = m->F;
+            const int64_t nvv = m->rel[TG_REL_VV].entries;
+            const int64_t *vvo = m->rel[TG_REL_VV].off;
+            const int32_t *vvp = m->rel[TG_REL_VV].ent;
+            int32_t *eidv;
+            TRY(tmp.alloc(&eidv, nvv));
+            const bool need_ev = mask & (TG_EV | TG_EE);
+            const bool need_te = mask & (TG_TE | TG_FE);
+            const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF)) || want_tt_face;
+            const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
+            int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
+            if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
+            if (need_te) TRY(tmp.alloc(&te, 6 * T));
+            if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
+            if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
+            if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
+            int32_t *et_cnt = nullptr, *ef_cnt = nullptr, *ee_cnt = nullptr, *ff_cnt = nullptr,
+                    *tt_cnt = nullptr;
+            if (mask & TG_ET) TRY(tmp.alloc(&et_cnt, E));
+            if (mask & TG_EF) TRY(tmp.alloc(&ef_cnt, E));
+            if (mask & TG_EE) TRY(tmp.alloc(&ee_cnt, E));
+            if (mask & TG_FF) TRY(tmp.alloc(&ff_cnt, F));
+            if (want_tt_face) TRY(tmp.alloc(&tt_cnt, T, true));
+
+            StarB b{};
+            b.vt_off = vt_off; b.vt = vt; b.tvs = m->tvs;
+            b.vv_off = vvo; b.vv = vvp; b.vvmask = vvmask;
+            b.eflag = eflag; b.epre = epre; b.fflag = fflag; b.fpre = fpre;
+            b.V = V; b.eidv = eidv; b.ev = ev; b.te = te; b.tf = tf; b.fv = fv; b.ft = ft;
+            b.et_cnt = et_cnt; b.ef_cnt = ef_cnt; b.ee_cnt = ee_cnt; b.ff_cnt = ff_cnt;
+            b.tt_cnt = tt_cnt; b.st = m->st;
+            launch_star_b(b, s);
+
+            // CSR offsets of ET, EF, EE, FF, TT
+            ScanJob jobs[5];
+            int nj = 0;
+            int64_t *et_off = nullptr, *ef_off = nullptr, *ee_off = nullptr, *ff_off = nullptr,
+                    *tt_off = nullptr;
+            const void *src[5];
+            bool w8[5];
+            int which[5];
+            auto add = [&](int32_t *cnt, int64_t **off, int64_t n, int rel) -> tg_status {
+                if (!cnt) return TG_OK;
+                TRY(dalloc(off, n + 1, s));
+                jobs[nj] = {cnt, *off, n, SCAN_COUNT_I32, 0};
+                src[nj] = *off + n;
+                w8[nj] = true;
+                which[nj] = rel;
+                nj++;
+                return TG_OK;
+            };
+            TRY(add(et_cnt, &et_off, E, TG_REL_ET));
+            TRY(add(ef_cnt, &ef_off, E, TG_REL_EF));
+            TRY(add(ee_cnt, &ee_off, E, TG_REL_EE));
+            TRY(add(ff_cnt, &ff_off, F, TG_REL_FF));
+            TRY(add(tt_cnt, &tt_off, T, TG_REL_TT));
+            char *scratch2 = nullptr;
+            if (nj) {
+                TRY(tmp.alloc(&scratch2,
+                              nj * (int64_t)(scan_scratch_bytes(std::max(std::max(E, F), T)) + 256)));
+                scan_batch(jobs, nj, scratch2, s);
+            }
+            TRY(sync_read(m, s, nj, src, w8));
+            if (m->st_host->flags) return check_flags(m);
+            int64_t total[14] = {0};
+            for (int i = 0; i < nj; i++) total[which[i]] = m->sz_host[i];
+
+            int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
+                    *fe = nullptr;
+            if (et_off) TRY(dalloc(&et, total[TG_REL_ET], s));
+            if (ef_off) TRY(dalloc(&ef, total[TG_REL_EF], s));
+            if (ee_off) TRY(dalloc(&ee, total[TG_REL_EE], s));
+            if (ff_off) TRY(dalloc(&ff, total[TG_REL_FF], s));
+            if (tt_off) TRY(dalloc(&tt, total[TG_REL_TT], s));
+            if (mask & TG_FE) TRY(dalloc(&fe, 3 * F, s));
+
+            if (et || ef) {
+                StarC c{vt_off, vt, m->tvs, vvo, vvp, vvmask, eidv, fflag, fpre,
+                        V, et_off, et, ef_off, ef};
+                launch_star_c(c, s);
+            }
+            if (fe || tt) launch_cell_fe_tt(m->tvs, T, te, tf, ft, fe, tt_off, tt, s);
+            if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s);
+            if (ee) {
+                launch_sort_rows(vvo, eidv, V, s);  // incident edge ids, ascending
+                launch_ee_fill(ev, E, vvo, eidv, ee_off, ee, s);
+            }
+            CK(cudaGetLastError());
+
+            // hand requested outputs to the mesh
+            auto give_fixed = [&](int r, int32_t *p, int64_t rows) {
+                tmp.keep(p);
+                set_fixed(m, r, p, rows);
+            };
+            if (mask & TG_EV) give_fixed(TG_REL_EV, ev, E);
+            if (mask & TG_TE) give_fixed(TG_REL_TE, te, T);
+            if (mask & TG_TF) give_fixed(TG_REL_TF, tf, T);
+            if (mask & TG_FV) give_fixed(TG_REL_FV, fv, F);
+            if (mask & TG_FT) give_fixed(TG_REL_FT, ft, F);
+            if (mask & TG_FE) set_fixed(m, TG_REL_FE, fe, F);
+            if (et) set_csr(m, TG_REL_ET, et_off, et, E, total[TG_REL_ET]);
+            if (ef) set_csr(m, TG_REL_EF, ef_off, ef, E, total[TG_REL_EF]);
+            if (ee) set_csr(m, TG_REL_EE, ee_off, ee, E, total[TG_REL_EE]);
+            if (ff) set_csr(m, TG_REL_FF, ff_off, ff, F, total[TG_REL_FF]);
+            if (tt) set_csr(m, TG_REL_TT, tt_off, tt, T, total[TG_REL_TT], 0);
+        }
+    }
+
+    if ((mask & TG_TT) && tt_vertex) {
+        int32_t *cnt;
+        int64_t *tt_off;
+        TRY(tmp.alloc(&cnt, T));
+        TRY(dalloc(&tt_off, T + 1, s));
+        launch_tt_vertex_count(m->tvs, T, vt_off, vt, cnt, s);
+        char *scratch;
+        TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(T) + 256));
+        ScanJob job{cnt, tt_off, T, SCAN_COUNT_I32, 0};
+        scan_batch(&job, 1, scratch, s);
+        const void *src[1] = {tt_off + T};
+        const bool w8[1] = {true};
+        TRY(sync_read(m, s, 1, src, w8));
+        int32_t *tt;
+        TRY(dalloc(&tt, m->sz_host[0], s));
+        launch_tt_vertex_fill(m->tvs, T, vt_off, vt, tt_off, tt, s);
+        set_csr(m, TG_REL_TT, tt_off, tt, T, m->sz_host[0], TG_OPT_TT_VERTEX_SHARING);
+    }
+    CK(cudaGetLastError());
+    return TG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *tg_version(void) { return "tetragpu-gb300 1.0 (sm_103a)"; }
+
+const char *tg_last_error_string(void) { return g_err.c_str(); }
+
+int64_t tg_kernel_launch_count(void) { return tg::g_launches.load(); }
+
+tg_status tg_mesh_destroy(tg_mesh *m)
+{
+    if (!m) return TG_OK;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(m->device);
+    cudaDeviceSynchronize();
+    for (auto &r : m->rel) free_rel(r);
+    if (m->tvs) cudaFree(m->tvs);
+    if (m->cadj) cudaFree(m->cadj);
+    if (m->st) cudaFree(m->st);
+    if (m->st_host) cudaFreeHost(m->st_host);
+    if (m->sz_host) cudaFreeHost(m->sz_host);
+    cudaSetDevice(cur);
+    (void)cudaGetLastError();
+    delete m;
+    return TG_OK;
+}
+
+static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int on_device,
+                                  cudaStream_t s, tg_mesh *m)
+{
+    CK(cudaGetDevice(&m->device));
+    setup_pool(m->device);
+    CK(cudaMallocHost((void **)&m->st_host, sizeof(DevStatus)));
+    CK(cudaMallocHost((void **)&m->sz_host, 16 * sizeof(int64_t)));
+    CK(cudaMalloc((void **)&m->st, sizeof(DevStatus)));
+    TRY(reset_status(m, s));
+    TRY(dalloc(&m->tvs, T, s));
+    const int32_t *src = tv;
+    if (!on_device && T > 0) {
+        CK(cudaMemcpyAsync(m->tvs, tv, (size_t)T * 16, cudaMemcpyHostToDevice, s));
+        src = reinterpret_cast<const int32_t *>(m->tvs);
+    }
+    Temps tmp(s);
+    int32_t *deg_t;
+    TRY(tmp.alloc(&deg_t, V, true));
+    launch_canon(src, T, V, m->tvs, deg_t, m->st, s);
+    int64_t *vt_off;
+    int32_t *vt;
+    TRY(dalloc(&vt_off, V + 1, s));
+    char *scratch;
+    TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(V) + 256));
+    ScanJob job{deg_t, vt_off, V, SCAN_COUNT_I32, 0};
+    scan_batch(&job, 1, scratch, s);
+    CK(cudaMemsetAsync(deg_t, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
+    TRY(dalloc(&vt, 4 * T, s));
+    launch_vt_fill(m->tvs, T, vt_off, deg_t, vt, s);
+    launch_sort_rows(vt_off, vt, V, s);
+    CK(cudaGetLastError());
+    set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
+    TRY(sync_read(m, s, 0, nullptr, nullptr));
+    return check_flags(m);
+}
+
+tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts, int tv_on_device,
+                         void *stream, tg_mesh **out)
+{
+    if (!out) return fail(TG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (n_cells < 0 || n_verts < 0 || (n_cells > 0 && !tv))
+        return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh sizes or NULL TV");
+    if (n_cells > kMaxCells)
+        return fail(TG_ERR_UNSUPPORTED, "more than %lld cells (occurrence ids use 31 bits)",
+                    (long long)kMaxCells);
+    if (n_verts > INT_MAX) return fail(TG_ERR_UNSUPPORTED, "more than 2^31-1 vertices");
+    tg_mesh *m = new tg_mesh();
+    m->V = n_verts;
+    m->T = n_cells;
+    tg_status st = mesh_create_impl(tv, n_cells, n_verts, tv_on_device, (cudaStream_t)stream, m);
+    if (st != TG_OK) {
+        std::string keep = g_err;
+        tg_mesh_destroy(m);
+        g_err = keep;
+        return st;
+    }
+    *out = m;
+    return TG_OK;
+}
+
+tg_status tg_extract(tg_mesh *m, uint32_t mask, uint32_t options, void *stream)
+{
+    if (!m) return fail(TG_ERR_INVALID_ARGUMENT, "mesh is NULL");
+    mask &= TG_ALL_RELATIONS;
+    bool all_ready = true;
+    for (int r = 1; r < 14; r++)
+        if ((mask & bit(r)) && !(m->rel[r].ready && (r != TG_REL_TT || m->rel[r].opts ==
+                                                     (options & TG_OPT_TT_VERTEX_SHARING))))
+            all_ready = false;
+    if (all_ready) return TG_OK;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != m->device) CK(cudaSetDevice(m->device));
+    tg_status st = run_extract(m, mask, options, (cudaStream_t)stream);
+    if (cur != m->device) cudaSetDevice(cur);
+    return st;
+}
+
+tg_status tg_mesh_counts(const tg_mesh *m, int64_t *nv, int64_t *ne, int64_t *nf, int64_t *nc)
+{
+    if (!m) return fail(TG_ERR_INVALID_ARGUMENT, "mesh is NULL");
+    if (nv) *nv = m->V;
+    if (ne) *ne = m->E;
+    if (nf) *nf = m->F;
+    if (nc) *nc = m->T;
+    return TG_OK;
+}
+
+tg_status tg_get_relation(const tg_mesh *m, int r, const int64_t **off, const int32_t **ent,
+                          int64_t *rows, int64_t *entries, int32_t *width)
+{
+    if (!m || r < 1 || r > 13) return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh or relation index");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    if (off) *off = x.off;
+    if (ent) *ent = x.ent;
+    if (rows) *rows = x.rows;
+    if (entries) *entries = x.entries;
+    if (width) *width = x.width;
+    return TG_OK;
+}
+
+tg_status tg_copy_relation(const tg_mesh *m, int r, int64_t *off_host, int32_t *ent_host,
+                           void *stream)
+{
+    if (!m || r < 1 || r > 13) return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh or relation index");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (off_host && x.off)
+        CK(cudaMemcpyAsync(off_host, x.off, (size_t)(x.rows + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (ent_host && x.entries)
+        CK(cudaMemcpyAsync(ent_host, x.ent, (size_t)x.entries * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+
+tg_status tg_get_tv(const tg_mesh *m, const int32_t **tv)
+{
+    if (!m || !tv) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
+    *tv = reinterpret_cast<const int32_t *>(m->tvs);
+    return TG_OK;
+}
+
+tg_status tg_critical_points(tg_mesh *m, const void *field, int field_type, int field_on_device,
+                             uint32_t *classes_out, int out_on_device, void *stream)
+{
+    if (!m || !field || !classes_out) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (field_type != TG_FIELD_F32 && field_type != TG_FIELD_F64)
+        return fail(TG_ERR_INVALID_ARGUMENT, "field_type must be TG_FIELD_F32 or TG_FIELD_F64");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!m->rel[TG_REL_VV].ready) TRY(tg_extract(m, TG_VV, 0, stream));
+    const int64_t V = m->V;
+    const Rel &vv = m->rel[TG_REL_VV];
+    if (!m->cadj) {
+        TRY(reset_status(m, s));
+        TRY(dalloc(&m->cadj, vv.entries, s));
+        launch_crit_adj(vv.off, vv.ent, V, m->cadj, m->st, s);
+        TRY(sync_read(m, s, 0, nullptr, nullptr));
+        if (m->st_host->flags) {
+            cudaFree(m->cadj);
+            m->cadj = nullptr;
+            return check_flags(m);
+        }
+    }
+    Temps tmp(s);
+    const size_t esz = field_type == TG_FIELD_F64 ? 8 : 4;
+    const void *f = field;
+    if (!field_on_device) {
+        char *d;
+        TRY(tmp.alloc(&d, (int64_t)(V * esz)));
+        CK(cudaMemcpyAsync(d, field, V * esz, cudaMemcpyHostToDevice, s));
+        f = d;
+    }
+    uint32_t *out = classes_out;
+    if (!out_on_device) TRY(tmp.alloc(&out, 3 * V));
+    launch_crit_classify(vv.off, vv.ent, m->cadj, f, field_type, V, out, s);
+    CK(cudaGetLastError());
+    if (!out_on_device) {
+        CK(cudaMemcpyAsync(classes_out, out, (size_t)V * 12, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return TG_OK;
+}
+
+tg_status tg_profile_kernel(const char *name)
+{
+    std::lock_guard<std::mutex> lk(tg::g_prof_mu);
+    tg::g_prof_name = name ? name : "";
+    tg::g_prof_on.store(!tg::g_prof_name.empty());
+    return TG_OK;
+}
+
+tg_status tg_profile_read(double *total_ms, int64_t *launches, int reset)
+{
+    std::lock_guard<std::mutex> lk(tg::g_prof_mu);
+    double ms = 0.0;
+    for (auto &p : tg::g_prof_events) {
+        CK(cudaEventSynchronize(p.b));
+        float x = 0.f;
+        CK(cudaEventElapsedTime(&x, p.a, p.b));
+        ms += x;
+    }
+    if (total_ms) *total_ms = ms;
+    if (launches) *launches = (int64_t)tg::g_prof_events.size();
+    if (reset) {
+        for (auto &p : tg::g_prof_events) {
+            tg::g_prof_pool.push_back(p.a);
+            tg::g_prof_pool.push_back(p.b);
+        }
+        tg::g_prof_events.clear();
+    }
+    return TG_OK;
+}
+
+int64_t tg_mesh_device_bytes(const tg_mesh *m)
+{
+    if (!m) return 0;
+    int64_t b = m->T * 16;
+    for (int r = 1; r < 14; r++) {
+        const Rel &x = m->rel[r];
+        if (!x.ready) continue;
+        b += x.entries * 4;
+        if (x.off) b += (x.rows + 1) * 8;
+    }
+    if (m->cadj) b += m->rel[TG_REL_VV].entries * 8;
+    return b;
+}
+
+}  // extern "C"
