@@ -126,6 +126,33 @@ void setup_pool(int dev)
     g_pool_ready[dev] = true;
 }
 
+// Pinned host slots for the status word and the sizes read back at the
+// synchronisation points: pinned allocation is slow, so slots come from a
+// process-wide pool of 4 KiB chunks and are recycled.
+struct PinnedPool {
+    std::mutex mu;
+    std::vector<void *> free_slots;
+    void *get()
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (free_slots.empty()) {
+            char *chunk = nullptr;
+            if (cudaMallocHost((void **)&chunk, 4096) != cudaSuccess) return nullptr;
+            for (int i = 0; i < 16; i++) free_slots.push_back(chunk + 256 * i);
+        }
+        void *p = free_slots.back();
+        free_slots.pop_back();
+        return p;
+    }
+    void put(void *p)
+    {
+        if (!p) return;
+        std::lock_guard<std::mutex> lk(mu);
+        free_slots.push_back(p);
+    }
+};
+PinnedPool g_pinned;
+
 struct Rel {
     int64_t rows = 0, entries = 0;
     int width = 0;
@@ -186,10 +213,14 @@ tg_status dalloc(T **out, int64_t count, cudaStream_t s)
 
 }  // namespace
 
+void tg::set_last_error(const char *msg) { g_err = msg; }
+
 struct tg_mesh {
     int device = 0;
+    cudaStream_t last_stream = nullptr;  // stream of the last call, used to free asynchronously
     int64_t V = 0, T = 0, E = -1, F = -1;
     int4 *tvs = nullptr;
+    int32_t *vt_win = nullptr;          // VT window table (window_count + 1 entries)
     Rel rel[14];
     uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
     DevStatus *st = nullptr;    // device
@@ -199,23 +230,21 @@ struct tg_mesh {
 
 namespace {
 
-void free_rel(Rel &r)
+void free_rel(Rel &r, cudaStream_t s = nullptr, bool async = false)
 {
-    if (r.off) cudaFree(r.off);
-    if (r.ent) cudaFree(r.ent);
+    if (async) {
+        if (r.off) cudaFreeAsync(r.off, s);
+        if (r.ent) cudaFreeAsync(r.ent, s);
+    } else {
+        if (r.off) cudaFree(r.off);
+        if (r.ent) cudaFree(r.ent);
+    }
     r = Rel();
 }
 
 tg_status reset_status(tg_mesh *m, cudaStream_t s)
 {
-    DevStatus init{};
-    init.flags = 0;
-    init.bad_cell = INT_MAX;
-    init.bad_vertex = INT_MAX;
-    CK(cudaStreamSynchronize(s));  // st_host may still be the source of an earlier copy
-    *m->st_host = init;
-    CK(cudaMemcpyAsync(m->st, m->st_host, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
+    launch_reset_status(m->st, s);
     return TG_OK;
 }
 
@@ -292,185 +321,174 @@ void set_csr(tg_mesh *m, int r, int64_t *off, int32_t *ent, int64_t rows, int64_
 
 tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
 {
-    const int64_t V = m->V, T = m->T;
+    const int64_t V = m->V, T = m->T, NVT = 4 * T;
     const bool tt_vertex = (opts & TG_OPT_TT_VERTEX_SHARING) != 0;
     const bool want_tt_face = (mask & TG_TT) && !tt_vertex;
-    const uint32_t starb_rel = TG_TE | TG_EV | TG_ET | TG_TF | TG_FV | TG_FE | TG_FT | TG_EF |
-                               TG_FF | TG_EE;
-    const bool want_b = (mask & starb_rel) || want_tt_face;
-    const bool want_vv = want_b || (mask & TG_VV);
+    const uint32_t star_rel = TG_TE | TG_EV | TG_ET | TG_TF | TG_FV | TG_FE | TG_FT | TG_EF |
+                              TG_FF | TG_EE | TG_VV;
+    const bool want_star = (mask & star_rel) || want_tt_face;
     const int64_t *vt_off = m->rel[TG_REL_VT].off;
     const int32_t *vt = m->rel[TG_REL_VT].ent;
     Temps tmp(s);
 
-    if (want_vv) {
+    if (want_star) {
         TRY(reset_status(m, s));
+        // ---- pass A: first occurrences, neighbour counts, ET/EF row lengths ----
         const int64_t nwe = (6 * T + 31) / 32, nwf = (4 * T + 31) / 32;
-        uint32_t *eflag, *fflag;
-        int32_t *epre, *fpre, *deg;
+        uint32_t *eflag, *fflag, *fbnd;
+        uint2 *erank, *frank, *brank;
+        uint16_t *ecnt = nullptr;
+        int32_t *deg;
         int64_t *vv_off;
-        TRY(tmp.alloc(&eflag, nwe));
-        TRY(tmp.alloc(&fflag, nwf));
-        TRY(tmp.alloc(&epre, nwe + 1));
-        TRY(tmp.alloc(&fpre, nwf + 1));
+        const bool need_ecnt = mask & (TG_ET | TG_EF | TG_EE);
+        TRY(tmp.alloc(&eflag, nwe, true));
+        TRY(tmp.alloc(&fflag, nwf, true));
+        TRY(tmp.alloc(&fbnd, nwf, true));
+        TRY(tmp.alloc(&erank, nwe + 1));
+        TRY(tmp.alloc(&frank, nwf + 1));
+        TRY(tmp.alloc(&brank, nwf + 1));
+        if (need_ecnt) TRY(tmp.alloc(&ecnt, 6 * T, true));
         TRY(tmp.alloc(&deg, V));
         TRY(dalloc(&vv_off, V + 1, s));
+        tmp.p[tmp.n++] = vv_off;  // owned by the VV relation once it is ready
         char *scratch;
         const int64_t maxn = std::max(V, std::max(nwe, nwf));
-        TRY(tmp.alloc(&scratch, 3 * (int64_t)(scan_scratch_bytes(maxn) + 256)));
-
-        int32_t *sum_nb = nullptr;
-        uint64_t *sum_mask = nullptr;
-        uint64_t *vvmask = nullptr;
-        int wide = 0;
-        for (int attempt = 0; attempt < 2; attempt++) {
-            const int64_t cap = wide ? 3 * 4 * T : 4 * T + 2 * V;
-            Temps sum(s);
-            TRY(sum.alloc(&sum_nb, cap));
-            TRY(sum.alloc(&sum_mask, cap));
-            CK(cudaMemsetAsync(eflag, 0, nwe * 4, s));
-            CK(cudaMemsetAsync(fflag, 0, nwf * 4, s));
-            StarA a{vt_off, vt, m->tvs, V, deg, sum_nb, sum_mask, eflag, fflag, m->st, wide};
-            launch_star_a(a, s);
-            ScanJob jobs[3] = {{deg, vv_off, V, SCAN_COUNT_I32, 0},
-                               {eflag, epre, nwe, SCAN_POPC_U32, 0},
-                               {fflag, fpre, nwf, SCAN_POPC_U32, 0}};
-            scan_batch(jobs, 3, scratch, s);
-            const void *src[3] = {vv_off + V, epre + nwe, fpre + nwf};
-            const bool w8[3] = {true, false, false};
-            TRY(sync_read(m, s, 3, src, w8));
-            if ((m->st_host->flags & ST_STAR_OVERFLOW) && !wide &&
-                !(m->st_host->flags & ~ST_STAR_OVERFLOW)) {
-                // a non-manifold vertex: redo with the always-sufficient capacity
-                wide = 1;
-                TRY(reset_status(m, s));
-                continue;
-            }
-            if (m->st_host->flags) {
-                cudaFreeAsync(vv_off, s);
-                return check_flags(m);
-            }
-            const int64_t nvv = m->sz_host[0];
-            m->E = m->sz_host[1];
-            m->F = m->sz_host[2];
-            int32_t *vv;
-            TRY(dalloc(&vv, nvv, s));
-            TRY(tmp.alloc(&vvmask, nvv));
-            launch_vv_finalize(vt_off, sum_nb, sum_mask, vv_off, V, wide, vv, vvmask, s);
-            set_csr(m, TG_REL_VV, vv_off, vv, V, nvv);
-            if (m->cadj) {
-                cudaFreeAsync(m->cadj, s);
-                m->cadj = nullptr;
-            }
-            break;
+        TRY(tmp.alloc(&scratch, 5 * (int64_t)(scan_scratch_bytes(maxn) + 256)));
+        int64_t *deg_sq;  // prefix of deg^2: its total sizes EE (sum deg^2 - 2E)
+        TRY(tmp.alloc(&deg_sq, V + 1));
+        StarA a{vt_off, m->vt_win, vt, m->tvs, V, NVT, deg, ecnt, eflag, fflag, fbnd, m->st};
+        if (!ecnt) {
+            // pass A always records row lengths; give it a throwaway buffer
+            TRY(tmp.alloc(&ecnt, 6 * T));
+            a.ecnt = ecnt;
         }
-        if (want_b) {
-            const int64_t E = m->E, F = m->F;
-            const int64_t nvv = m->rel[TG_REL_VV].entries;
-            const int64_t *vvo = m->rel[TG_REL_VV].off;
-            const int32_t *vvp = m->rel[TG_REL_VV].ent;
-            int32_t *eidv;
-            TRY(tmp.alloc(&eidv, nvv));
-            const bool need_ev = mask & (TG_EV | TG_EE);
-            const bool need_te = mask & (TG_TE | TG_FE);
-            const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF)) || want_tt_face;
-            const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
-            int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
-            if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
-            if (need_te) TRY(tmp.alloc(&te, 6 * T));
-            if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
-            if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
-            if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
-            int32_t *et_cnt = nullptr, *ef_cnt = nullptr, *ee_cnt = nullptr, *ff_cnt = nullptr,
-                    *tt_cnt = nullptr;
-            if (mask & TG_ET) TRY(tmp.alloc(&et_cnt, E));
-            if (mask & TG_EF) TRY(tmp.alloc(&ef_cnt, E));
-            if (mask & TG_EE) TRY(tmp.alloc(&ee_cnt, E));
-            if (mask & TG_FF) TRY(tmp.alloc(&ff_cnt, F));
-            if (want_tt_face) TRY(tmp.alloc(&tt_cnt, T, true));
+        launch_star_a(a, s);
+        ScanJob jobs[5] = {{deg, vv_off, V, SCAN_COUNT_I32, 0},
+                           {eflag, erank, nwe, SCAN_POPC_RANK, 0},
+                           {fflag, frank, nwf, SCAN_POPC_RANK, 0},
+                           {fbnd, brank, nwf, SCAN_POPC_RANK, 0},
+                           {deg, deg_sq, V, SCAN_SQUARE_I32, 0}};
+        scan_batch(jobs, 5, scratch, s);
 
-            StarB b{};
-            b.vt_off = vt_off; b.vt = vt; b.tvs = m->tvs;
-            b.vv_off = vvo; b.vv = vvp; b.vvmask = vvmask;
-            b.eflag = eflag; b.epre = epre; b.fflag = fflag; b.fpre = fpre;
-            b.V = V; b.eidv = eidv; b.ev = ev; b.te = te; b.tf = tf; b.fv = fv; b.ft = ft;
-            b.et_cnt = et_cnt; b.ef_cnt = ef_cnt; b.ee_cnt = ee_cnt; b.ff_cnt = ff_cnt;
-            b.tt_cnt = tt_cnt; b.st = m->st;
-            launch_star_b(b, s);
-
-            // CSR offsets of ET, EF, EE, FF, TT
-            ScanJob jobs[5];
-            int nj = 0;
-            int64_t *et_off = nullptr, *ef_off = nullptr, *ee_off = nullptr, *ff_off = nullptr,
-                    *tt_off = nullptr;
-            const void *src[5];
-            bool w8[5];
-            int which[5];
-            auto add = [&](int32_t *cnt, int64_t **off, int64_t n, int rel) -> tg_status {
-                if (!cnt) return TG_OK;
-                TRY(dalloc(off, n + 1, s));
-                jobs[nj] = {cnt, *off, n, SCAN_COUNT_I32, 0};
-                src[nj] = *off + n;
-                w8[nj] = true;
-                which[nj] = rel;
-                nj++;
-                return TG_OK;
-            };
-            TRY(add(et_cnt, &et_off, E, TG_REL_ET));
-            TRY(add(ef_cnt, &ef_off, E, TG_REL_EF));
-            TRY(add(ee_cnt, &ee_off, E, TG_REL_EE));
-            TRY(add(ff_cnt, &ff_off, F, TG_REL_FF));
-            TRY(add(tt_cnt, &tt_off, T, TG_REL_TT));
-            char *scratch2 = nullptr;
-            if (nj) {
-                TRY(tmp.alloc(&scratch2,
-                              nj * (int64_t)(scan_scratch_bytes(std::max(std::max(E, F), T)) + 256)));
-                scan_batch(jobs, nj, scratch2, s);
-            }
-            TRY(sync_read(m, s, nj, src, w8));
-            if (m->st_host->flags) return check_flags(m);
-            int64_t total[14] = {0};
-            for (int i = 0; i < nj; i++) total[which[i]] = m->sz_host[i];
-
-            int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
-                    *fe = nullptr;
-            if (et_off) TRY(dalloc(&et, total[TG_REL_ET], s));
-            if (ef_off) TRY(dalloc(&ef, total[TG_REL_EF], s));
-            if (ee_off) TRY(dalloc(&ee, total[TG_REL_EE], s));
-            if (ff_off) TRY(dalloc(&ff, total[TG_REL_FF], s));
-            if (tt_off) TRY(dalloc(&tt, total[TG_REL_TT], s));
-            if (mask & TG_FE) TRY(dalloc(&fe, 3 * F, s));
-
-            if (et || ef) {
-                StarC c{vt_off, vt, m->tvs, vvo, vvp, vvmask, eidv, fflag, fpre,
-                        V, et_off, et, ef_off, ef};
-                launch_star_c(c, s);
-            }
-            if (fe || tt) launch_cell_fe_tt(m->tvs, T, te, tf, ft, fe, tt_off, tt, s);
-            if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s);
-            if (ee) {
-                launch_sort_rows(vvo, eidv, V, s);  // incident edge ids, ascending
-                launch_ee_fill(ev, E, vvo, eidv, ee_off, ee, s);
-            }
-            CK(cudaGetLastError());
-
-            // hand requested outputs to the mesh
-            auto give_fixed = [&](int r, int32_t *p, int64_t rows) {
-                tmp.keep(p);
-                set_fixed(m, r, p, rows);
-            };
-            if (mask & TG_EV) give_fixed(TG_REL_EV, ev, E);
-            if (mask & TG_TE) give_fixed(TG_REL_TE, te, T);
-            if (mask & TG_TF) give_fixed(TG_REL_TF, tf, T);
-            if (mask & TG_FV) give_fixed(TG_REL_FV, fv, F);
-            if (mask & TG_FT) give_fixed(TG_REL_FT, ft, F);
-            if (mask & TG_FE) set_fixed(m, TG_REL_FE, fe, F);
-            if (et) set_csr(m, TG_REL_ET, et_off, et, E, total[TG_REL_ET]);
-            if (ef) set_csr(m, TG_REL_EF, ef_off, ef, E, total[TG_REL_EF]);
-            if (ee) set_csr(m, TG_REL_EE, ee_off, ee, E, total[TG_REL_EE]);
-            if (ff) set_csr(m, TG_REL_FF, ff_off, ff, F, total[TG_REL_FF]);
-            if (tt) set_csr(m, TG_REL_TT, tt_off, tt, T, total[TG_REL_TT], 0);
+        // ---- the one synchronisation: edge, face, neighbour and boundary
+        // counts size every output from here on ----
+        {
+            const void *src[5] = {vv_off + V, &erank[nwe].y, &frank[nwf].y, &brank[nwf].y,
+                                  deg_sq + V};
+            const bool w8[5] = {true, false, false, false, true};
+            TRY(sync_read(m, s, 5, src, w8));
         }
+        if (m->st_host->flags) return check_flags(m);
+        const int64_t nvv = m->sz_host[0];
+        const int64_t E = m->sz_host[1], F = m->sz_host[2];
+        const int64_t n_bnd = m->sz_host[3];  // boundary faces
+        const int64_t sum_deg_sq = m->sz_host[4];
+        m->E = E;
+        m->F = F;
+        int64_t *et_off = nullptr, *ef_off = nullptr, *ee_off = nullptr;
+        if (mask & TG_ET) TRY(dalloc(&et_off, E + 1, s));
+        if (mask & TG_EF) TRY(dalloc(&ef_off, E + 1, s));
+        if (mask & TG_EE) TRY(dalloc(&ee_off, E + 1, s));
+        if (et_off) tmp.p[tmp.n++] = et_off;
+        if (ef_off) tmp.p[tmp.n++] = ef_off;
+        if (ee_off) tmp.p[tmp.n++] = ee_off;
+        if (et_off || ef_off || ee_off) {
+            char *scratch2;
+            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T) + 256));
+            launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
+                                scratch2, s);
+        }
+
+        // ---- pass B: ids, VV, fixed-width relations, ET and EF rows ----
+        const bool need_ev = mask & (TG_EV | TG_EE);
+        const bool need_te = mask & (TG_TE | TG_FE);
+        const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF)) || want_tt_face;
+        const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
+        int32_t *vv, *eidv, *eid_sorted = nullptr;
+        int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
+        int64_t *ff_off = nullptr;
+        TRY(dalloc(&vv, nvv, s));
+        tmp.p[tmp.n++] = vv;
+        TRY(tmp.alloc(&eidv, nvv));
+        if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
+        if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
+        if (need_te) TRY(tmp.alloc(&te, 6 * T));
+        if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
+        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
+        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
+        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
+        // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
+        // only when EE is wanted); TT and FF from the boundary-face count
+        int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
+                *fe = nullptr;
+        int64_t *tt_off = nullptr;
+        const int64_t n_et = 6 * T, n_ef = 3 * F;
+        const int64_t n_tt = 4 * T - n_bnd, n_ff = 3 * (2 * F - n_bnd);
+        if (et_off) TRY(dalloc(&et, n_et, s));
+        if (ef_off) TRY(dalloc(&ef, n_ef, s));
+        if (mask & TG_FE) TRY(dalloc(&fe, 3 * F, s));
+        if (want_tt_face) {
+            TRY(dalloc(&tt_off, T + 1, s));
+            TRY(dalloc(&tt, n_tt, s));
+            if (T == 0) CK(cudaMemsetAsync(tt_off, 0, 8, s));
+        }
+        if (mask & TG_FF) {
+            TRY(dalloc(&ff, n_ff, s));
+            if (T == 0) CK(cudaMemsetAsync(ff_off, 0, 8, s));
+        }
+        StarB b{};
+        b.vt_off = vt_off; b.win = m->vt_win; b.vt = vt; b.tvs = m->tvs; b.V = V; b.nvt = NVT;
+        b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
+        b.vv = vv; b.eidv = eidv; b.eid_sorted = eid_sorted;
+        b.ev = ev; b.te = te; b.tf = tf; b.fv = fv; b.ft = ft; b.ff_off = ff_off;
+        b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
+        launch_star_b(b, s);
+        tmp.keep(vv);
+        tmp.keep(vv_off);
+        set_csr(m, TG_REL_VV, vv_off, vv, V, nvv);
+        if (m->cadj) {
+            cudaFreeAsync(m->cadj, s);
+            m->cadj = nullptr;
+        }
+
+        if (fe || tt || ff_off)
+            launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s);
+        if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s);
+        // an edge (a,b) has deg(a) + deg(b) - 2 EE entries: sum deg^2 - 2E in all
+        const int64_t n_ee = sum_deg_sq - 2 * E;
+        if (ee_off) {
+            TRY(dalloc(&ee, n_ee, s));
+            launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+        }
+        CK(cudaGetLastError());
+
+        auto give_fixed = [&](int r, int32_t *p, int64_t rows) {
+            tmp.keep(p);
+            set_fixed(m, r, p, rows);
+        };
+        if (mask & TG_EV) give_fixed(TG_REL_EV, ev, E);
+        if (mask & TG_TE) give_fixed(TG_REL_TE, te, T);
+        if (mask & TG_TF) give_fixed(TG_REL_TF, tf, T);
+        if (mask & TG_FV) give_fixed(TG_REL_FV, fv, F);
+        if (mask & TG_FT) give_fixed(TG_REL_FT, ft, F);
+        if (fe) set_fixed(m, TG_REL_FE, fe, F);
+        if (et) {
+            tmp.keep(et_off);
+            set_csr(m, TG_REL_ET, et_off, et, E, n_et);
+        }
+        if (ef) {
+            tmp.keep(ef_off);
+            set_csr(m, TG_REL_EF, ef_off, ef, E, n_ef);
+        }
+        if (ee) {
+            tmp.keep(ee_off);
+            set_csr(m, TG_REL_EE, ee_off, ee, E, n_ee);
+        }
+        if (ff) {
+            tmp.keep(ff_off);
+            set_csr(m, TG_REL_FF, ff_off, ff, F, n_ff);
+        }
+        if (tt) set_csr(m, TG_REL_TT, tt_off, tt, T, n_tt, 0);
     }
 
     if ((mask & TG_TT) && tt_vertex) {
@@ -511,13 +529,17 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(m->device);
-    cudaDeviceSynchronize();
-    for (auto &r : m->rel) free_rel(r);
-    if (m->tvs) cudaFree(m->tvs);
-    if (m->cadj) cudaFree(m->cadj);
-    if (m->st) cudaFree(m->st);
-    if (m->st_host) cudaFreeHost(m->st_host);
-    if (m->sz_host) cudaFreeHost(m->sz_host);
+    // stream-ordered frees on the stream the mesh was last used on, then one
+    // wait for that stream (no device-wide synchronisation)
+    cudaStream_t s = m->last_stream;
+    for (auto &r : m->rel) free_rel(r, s, true);
+    if (m->tvs) cudaFreeAsync(m->tvs, s);
+    if (m->vt_win) cudaFreeAsync(m->vt_win, s);
+    if (m->cadj) cudaFreeAsync(m->cadj, s);
+    if (m->st) cudaFreeAsync(m->st, s);
+    cudaStreamSynchronize(s);  // no copy into the pinned slots is still in flight
+    g_pinned.put(m->st_host);
+    g_pinned.put(m->sz_host);
     cudaSetDevice(cur);
     (void)cudaGetLastError();
     delete m;
@@ -529,9 +551,10 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
 {
     CK(cudaGetDevice(&m->device));
     setup_pool(m->device);
-    CK(cudaMallocHost((void **)&m->st_host, sizeof(DevStatus)));
-    CK(cudaMallocHost((void **)&m->sz_host, 16 * sizeof(int64_t)));
-    CK(cudaMalloc((void **)&m->st, sizeof(DevStatus)));
+    m->st_host = (DevStatus *)g_pinned.get();
+    m->sz_host = (int64_t *)g_pinned.get();
+    if (!m->st_host || !m->sz_host) return fail(TG_ERR_OUT_OF_MEMORY, "pinned host memory");
+    TRY(dalloc(&m->st, 1, s));
     TRY(reset_status(m, s));
     TRY(dalloc(&m->tvs, T, s));
     const int32_t *src = tv;
@@ -553,7 +576,9 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     CK(cudaMemsetAsync(deg_t, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
     TRY(dalloc(&vt, 4 * T, s));
     launch_vt_fill(m->tvs, T, vt_off, deg_t, vt, s);
-    launch_sort_rows(vt_off, vt, V, s);
+    TRY(dalloc(&m->vt_win, window_count(4 * T) + 1, s));
+    launch_window_starts(vt_off, V, 4 * T, m->vt_win, s);
+    launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, s);
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
     TRY(sync_read(m, s, 0, nullptr, nullptr));
@@ -574,6 +599,7 @@ tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts, in
     tg_mesh *m = new tg_mesh();
     m->V = n_verts;
     m->T = n_cells;
+    m->last_stream = (cudaStream_t)stream;
     tg_status st = mesh_create_impl(tv, n_cells, n_verts, tv_on_device, (cudaStream_t)stream, m);
     if (st != TG_OK) {
         std::string keep = g_err;
@@ -598,6 +624,7 @@ tg_status tg_extract(tg_mesh *m, uint32_t mask, uint32_t options, void *stream)
     int cur = 0;
     cudaGetDevice(&cur);
     if (cur != m->device) CK(cudaSetDevice(m->device));
+    m->last_stream = (cudaStream_t)stream;
     tg_status st = run_extract(m, mask, options, (cudaStream_t)stream);
     if (cur != m->device) cudaSetDevice(cur);
     return st;
@@ -656,19 +683,20 @@ tg_status tg_critical_points(tg_mesh *m, const void *field, int field_type, int 
     if (field_type != TG_FIELD_F32 && field_type != TG_FIELD_F64)
         return fail(TG_ERR_INVALID_ARGUMENT, "field_type must be TG_FIELD_F32 or TG_FIELD_F64");
     cudaStream_t s = (cudaStream_t)stream;
+    m->last_stream = s;
     if (!m->rel[TG_REL_VV].ready) TRY(tg_extract(m, TG_VV, 0, stream));
     const int64_t V = m->V;
     const Rel &vv = m->rel[TG_REL_VV];
     if (!m->cadj) {
         TRY(reset_status(m, s));
         TRY(dalloc(&m->cadj, vv.entries, s));
-        launch_crit_adj(vv.off, vv.ent, V, m->cadj, m->st, s);
-        TRY(sync_read(m, s, 0, nullptr, nullptr));
-        if (m->st_host->flags) {
-            cudaFree(m->cadj);
-            m->cadj = nullptr;
-            return check_flags(m);
-        }
+        int32_t *vv_win;
+        TRY(dalloc(&vv_win, window_count(vv.entries) + 1, s));
+        launch_window_starts(vv.off, V, vv.entries, vv_win, s);
+        // VV rows longer than the adjacency masks were already rejected by
+        // tg_extract (star pass A flags them), so no status read-back here
+        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st, s);
+        cudaFreeAsync(vv_win, s);
     }
     Temps tmp(s);
     const size_t esz = field_type == TG_FIELD_F64 ? 8 : 4;

@@ -12,8 +12,8 @@
 //
 // Two kernels, so that a second field on the same mesh reuses the first:
 //   k_crit_adj       field-independent: for every VV entry (v, u), the bitmask
-//                    of v's neighbours adjacent to u (merge of two sorted
-//                    rows).  Thread per vertex.
+//                    of v's neighbours adjacent to u.  Thread per VV entry,
+//                    v's row staged in shared memory.
 //   k_crit_classify  field-dependent: lower/upper split, then a union-find
 //                    with path halving in shared memory over the adjacency
 //                    bits of same-kind neighbours; roots are counted.
@@ -22,38 +22,67 @@
 namespace tg {
 namespace {
 
-__global__ void __launch_bounds__(128)
-k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t V,
-           unsigned long long *__restrict__ adj, DevStatus *st)
+// Link adjacency, thread per VV entry (v, u): bit j of the mask is set when
+// v's j-th neighbour is also a neighbour of u.  A block takes the vertices
+// whose VV rows start in a 256-entry window (win), stages those rows in
+// shared memory and scans each u's row from global memory against them.
+constexpr int kAdjWin = 256;
+constexpr int kAdjCap = kAdjWin + kMaxDeg;
+
+__global__ void __launch_bounds__(kAdjWin)
+k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
+           const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
 {
-    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
-    const int64_t b = vv_off[v];
-    const int n = (int)(vv_off[v + 1] - b);
-    if (n > kMaxDeg) {
-        atomicOr(&st->flags, ST_HEAVY_DEG);
-        atomicMin(&st->bad_vertex, (int)v);
+    __shared__ int nb[kAdjCap];
+    __shared__ int meta[kAdjCap];   // row start | row length << 16
+    __shared__ int s_vlo, s_vhi, s_n;
+    __shared__ long long s_base;
+    if (threadIdx.x == 0) {
+        s_vlo = win[blockIdx.x];
+        s_vhi = win[blockIdx.x + 1];
+        s_base = vv_off[s_vlo];
+        s_n = (int)(vv_off[s_vhi] - s_base);
+    }
+    __syncthreads();
+    const int n = s_n;
+    const long long base = s_base;
+    if (n > kAdjCap) {  // a row longer than kMaxDeg lies in this window
+        if (threadIdx.x == 0) {
+            atomicOr(&st->flags, ST_HEAVY_DEG);
+            atomicMin(&st->bad_vertex, s_vlo);
+        }
         return;
     }
-    const int *row = vv + b;
-    for (int k = 0; k < n; k++) {
-        const int u = __ldg(row + k);
+    for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
+        const int rs = (int)(vv_off[v] - base);
+        const int d = (int)(vv_off[v + 1] - vv_off[v]);
+        if (d > kMaxDeg) {
+            atomicOr(&st->flags, ST_HEAVY_DEG);
+            atomicMin(&st->bad_vertex, v);
+        }
+        for (int i = 0; i < d; i++) meta[rs + i] = rs | (d << 16);
+    }
+    for (int e = threadIdx.x; e < n; e += blockDim.x) nb[e] = __ldg(vv + base + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int m = meta[e], rs = m & 0xffff, d = m >> 16;
+        if (d > kMaxDeg) continue;
+        const int *row = nb + rs;
+        const int u = nb[e];
         const int64_t ub = vv_off[u];
         const int un = (int)(vv_off[u + 1] - ub);
-        const int *urow = vv + ub;
         unsigned long long bits = 0ull;
-        int i = 0, j = 0;
-        while (i < un && j < n) {
-            const int x = __ldg(urow + i), y = __ldg(row + j);
-            if (x < y) i++;
-            else if (x > y) j++;
-            else {
-                bits |= 1ull << j;
-                i++;
-                j++;
+#pragma unroll 4
+        for (int i = 0; i < un; i++) {
+            const int w = __ldg(vv + ub + i);
+            int lo = 0, hi = d;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (row[mid] < w) lo = mid + 1; else hi = mid;
             }
+            if (lo < d && row[lo] == w) bits |= 1ull << lo;
         }
-        adj[b + k] = bits;
+        adj[base + e] = bits;
     }
 }
 
@@ -126,15 +155,13 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 
 }  // namespace
 
-void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, int64_t V, uint64_t *adj,
-                     DevStatus *st, cudaStream_t s)
+void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s)
 {
     if (V == 0) return;
-    {
-        Launch L("k_crit_adj", s);
-        k_crit_adj<<<(unsigned)((V + 127) / 128), 128, 0, s>>>(
-            vv_off, vv, V, reinterpret_cast<unsigned long long *>(adj), st);
-    }
+    Launch L("k_crit_adj", s);
+    k_crit_adj<<<(unsigned)window_count(n_vv), kAdjWin, 0, s>>>(
+        vv_off, vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,

@@ -36,7 +36,9 @@ constexpr int kMaxDeg = 64;
 // ---- scans (tg_scan.cu) ----
 enum ScanKind : int {
     SCAN_COUNT_I32 = 0,  // in: int32 counts, out: int64 offsets [n + 1]
-    SCAN_POPC_U32 = 1    // in: uint32 bit words, out: int32 prefix of popcounts [n + 1]
+    SCAN_POPC_RANK = 1,  // in: uint32 bit words, out: uint2 {word, popcount prefix} [n + 1],
+                         //     out[n] = {0, total}: rank of bit p = one 8-byte load
+    SCAN_SQUARE_I32 = 2  // in: int32 x, out: int64 prefix of x*x [n + 1]
 };
 struct ScanJob {
     const void *in;
@@ -56,79 +58,77 @@ struct Sizes {
     int64_t V, T;
 };
 
+void launch_reset_status(DevStatus *st, cudaStream_t s);
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
                   DevStatus *st, cudaStream_t s);
 void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, int32_t *cursor,
                     int32_t *vt, cudaStream_t s);
 void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStream_t s);
+// Windows of 256 entries over a CSR: win[w] = first row starting at or after
+// entry 256 w (w = 0 .. window_count), win[window_count] = rows.
+int64_t window_count(int64_t n_entries);
+void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int32_t *win,
+                          cudaStream_t s);
+// sort every VT row (tg_star.cu): window-staged, coalesced
+void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
+                    int64_t nvt, cudaStream_t s);
 
 struct StarA {
     const int64_t *vt_off;
+    const int32_t *win;        // VT window table
     const int32_t *vt;
     const int4 *tvs;
     int64_t V;
-    int32_t *deg;          // [V] out
-    int32_t *sum_nb;       // padded summary, base vt_off[v] + 2v
-    uint64_t *sum_mask;
-    uint32_t *eflag;       // bit per edge occurrence 6c+j
-    uint32_t *fflag;       // bit per face occurrence 4c+k
+    int64_t nvt;               // VT entries (4 * cells)
+    int32_t *deg;              // [V] neighbour counts
+    uint16_t *ecnt;            // [6T] ET | EF << 8 row lengths at owned edges' first slots
+    uint32_t *eflag;           // bit per edge occurrence 6c+j (first occurrences)
+    uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
+    uint32_t *fbnd;            // bit per face occurrence: first and only (boundary face)
     DevStatus *st;
-    int wide;              // summary capacity 3D per vertex instead of D + 2
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
 
-void launch_vv_finalize(const int64_t *vt_off, const int32_t *sum_nb, const uint64_t *sum_mask,
-                        const int64_t *vv_off, int64_t V, int wide, int32_t *vv,
-                        uint64_t *vvmask, cudaStream_t s);
+// ET / EF / EE offsets in edge-id order from one scan over the 6T edge slots
+size_t edge_offsets_scratch_bytes(int64_t n_slots);
+void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
+                         const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
+                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, void *scratch,
+                         cudaStream_t s);
 
 struct StarB {
     const int64_t *vt_off;
+    const int32_t *win;        // VT window table
     const int32_t *vt;
     const int4 *tvs;
-    const int64_t *vv_off;
-    const int32_t *vv;
-    const uint64_t *vvmask;
-    const uint32_t *eflag;
-    const int32_t *epre;
-    const uint32_t *fflag;
-    const int32_t *fpre;
     int64_t V;
-    int32_t *eidv;     // [2E] edge id of every VV entry
-    int32_t *ev;       // [2E] or null
-    int32_t *te;       // [6T] or null
-    int32_t *tf;       // [4T] or null
-    int32_t *fv;       // [3F] or null
-    int32_t *ft;       // [2F] or null
-    int32_t *et_cnt;   // [E] or null
-    int32_t *ef_cnt;   // [E] or null
-    int32_t *ee_cnt;   // [E] or null
-    int32_t *ff_cnt;   // [F] or null
-    int32_t *tt_cnt;   // [T] or null (atomic adds; zeroed by the caller)
+    int64_t nvt;
+    const int64_t *vv_off;
+    const uint2 *erank;        // {bits, prefix} per 32 edge occurrences
+    const uint2 *frank;        // same for face occurrences
+    const uint2 *brank;        // same for boundary-face occurrences
+    int32_t *vv;               // [2E] VV rows
+    int32_t *eidv;             // [2E] edge id of every VV entry
+    int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null
+    int32_t *ev;               // [2E] or null
+    int32_t *te;               // [6T] or null
+    int32_t *tf;               // [4T] or null
+    int32_t *fv;               // [3F] or null
+    int32_t *ft;               // [2F] or null
+    int64_t *ff_off;           // [F+1] or null
+    const int64_t *et_off;
+    int32_t *et;               // or null
+    const int64_t *ef_off;
+    int32_t *ef;               // or null
     DevStatus *st;
 };
 void launch_star_b(const StarB &b, cudaStream_t s);
 
-struct StarC {
-    const int64_t *vt_off;
-    const int32_t *vt;
-    const int4 *tvs;
-    const int64_t *vv_off;
-    const int32_t *vv;
-    const uint64_t *vvmask;
-    const int32_t *eidv;
-    const uint32_t *fflag;
-    const int32_t *fpre;
-    int64_t V;
-    const int64_t *et_off;
-    int32_t *et;       // or null
-    const int64_t *ef_off;
-    int32_t *ef;       // or null
-};
-void launch_star_c(const StarC &c, cudaStream_t s);
-
-void launch_cell_fe_tt(const int4 *tvs, int64_t T, const int32_t *te, const int32_t *tf,
-                       const int32_t *ft, int32_t *fe, const int64_t *tt_off, int32_t *tt,
-                       cudaStream_t s);
+// FE of every face at its first cell; TT offsets (4c - boundary faces before
+// cell c), TT rows, and the closing FF offset.
+void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
+                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fe,
+                       int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
 void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64_t *ff_off,
                     int32_t *ff, cudaStream_t s);
 void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const int32_t *eid_sorted,
@@ -139,11 +139,15 @@ void launch_tt_vertex_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, co
                            const int64_t *tt_off, int32_t *tt, cudaStream_t s);
 
 // critical points (tg_crit.cu)
-void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, int64_t V, uint64_t *adj,
-                     DevStatus *st, cudaStream_t s);
+// vv_win: window table of VV (launch_window_starts over vv_off)
+void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s);
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
                           const void *field, int field_type, int64_t V, uint32_t *classes3,
                           cudaStream_t s);
+
+// the message tg_last_error_string returns on this thread
+void set_last_error(const char *msg);
 
 // launch accounting and optional CUDA-event timing of one named kernel
 void count_launch(int n = 1);

@@ -18,14 +18,7 @@
 //   k_canon        sort TV rows, validate ids, count cells per vertex
 //   k_vt_fill      scatter cells into VT rows (atomic cursors)
 //   k_sort_rows    sort each CSR row in place (VT, incident-edge rows)
-//   k_star_a       warp per vertex: distinct neighbours and the star positions
-//                  holding each (a 64-bit mask), via __match_any_sync and a
-//                  shared-memory hash; marks first occurrences of the edges
-//                  and faces the vertex owns (owner = lowest vertex)
-//   k_vv_finalize  thread per vertex: sort neighbours -> VV and masks
-//   k_star_b       warp per vertex: edge ids of all incident edges; EV, TE,
-//                  TF, FV, FT and the row counts of ET, EF, EE, FF, TT
-//   k_star_c       warp per vertex: ET and EF rows of owned edges
+//   k_star_a/b/c   the per-vertex star passes (tg_star.cu)
 //   k_cell_fe_tt   FE (from TE of a face's first cell) and face-sharing TT
 //   k_ff_fill      FF;  k_ee_fill  EE;  k_tt_vertex_*  vertex-sharing TT
 #include <climits>
@@ -100,10 +93,14 @@ k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, DevStatus *s
     } else {
         a = tv[4 * c]; b = tv[4 * c + 1]; d = tv[4 * c + 2]; e = tv[4 * c + 3];
     }
+    // A rejected cell is overwritten with -1s (the input may alias tvs) and
+    // takes no part in the counts; every later kernel skips it, and the host
+    // reports the error before anything reads the mesh again.
     if ((unsigned)a >= (unsigned)V || (unsigned)b >= (unsigned)V ||
         (unsigned)d >= (unsigned)V || (unsigned)e >= (unsigned)V) {
         atomicOr(&st->flags, ST_BAD_ID);
         atomicMin(&st->bad_cell, (int)c);
+        tvs[c] = make_int4(-1, -1, -1, -1);
         return;
     }
     TG_CSWAP(a, b);
@@ -114,6 +111,7 @@ k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, DevStatus *s
     if (a == b || b == d || d == e) {
         atomicOr(&st->flags, ST_DUP_VERTEX);
         atomicMin(&st->bad_cell, (int)c);
+        tvs[c] = make_int4(-1, -1, -1, -1);
         return;
     }
     tvs[c] = make_int4(a, b, d, e);
@@ -133,6 +131,7 @@ k_vt_fill(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__ v
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     const int4 w = tvs[c];
+    if (w.x < 0) return;  // rejected by k_canon
     vt[vt_off[w.x] + atomicAdd(cursor + w.x, 1)] = (int)c;
     vt[vt_off[w.y] + atomicAdd(cursor + w.y, 1)] = (int)c;
     vt[vt_off[w.z] + atomicAdd(cursor + w.z, 1)] = (int)c;
@@ -158,401 +157,30 @@ k_sort_rows(const int64_t *__restrict__ off, int *__restrict__ ent, int64_t n_ro
 }
 
 // ---------------------------------------------------------------------------
-// Star kernels: one warp per vertex, star positions in shared memory
-// ---------------------------------------------------------------------------
-constexpr int kWarps = 8;
-constexpr int kHash = 128;  // neighbour table slots per warp (>= 2 * kMaxDeg)
-
-struct StarTile {
-    int cell[kMaxStar];
-    int4 tv[kMaxStar];
-    signed char sv[kMaxStar];
-};
-
-__device__ __forceinline__ unsigned hash_slot(int u)
-{
-    return ((unsigned)u * 2654435761u) >> (32 - 7);
-}
-
-// Load the sorted star of v into shared memory (lanes stride positions).
-__device__ __forceinline__ void load_star(StarTile &t, const int *__restrict__ vt, int64_t b0, int D,
-                                          const int4 *__restrict__ tvs, int v, int lane)
-{
-    for (int i = lane; i < D; i += 32) {
-        const int c = __ldg(vt + b0 + i);
-        const int4 w = __ldg(tvs + c);
-        t.cell[i] = c;
-        t.tv[i] = w;
-        t.sv[i] = (signed char)slot_of(w, v);
-    }
-}
-
-struct SmemA {
-    StarTile t;
-    int hkey[kHash];
-    unsigned long long hmask[kHash];
-};
-
-__device__ __forceinline__ bool h_insert(int *hkey, unsigned long long *hmask, int u,
-                                         unsigned long long bits)
-{
-    unsigned h = hash_slot(u);
-    for (int probe = 0; probe < kHash; probe++) {
-        const int old = atomicCAS(hkey + h, -1, u);
-        if (old == -1 || old == u) {
-            atomicOr(hmask + h, bits);
-            return true;
-        }
-        h = (h + 1) & (kHash - 1);
-    }
-    return false;
-}
-
-__device__ __forceinline__ unsigned long long h_lookup(const int *hkey,
-                                                       const unsigned long long *hmask, int u)
-{
-    unsigned h = hash_slot(u);
-    for (int probe = 0; probe < kHash; probe++) {
-        const int k = hkey[h];
-        if (k == u) return hmask[h];
-        if (k == -1) return 0ull;
-        h = (h + 1) & (kHash - 1);
-    }
-    return 0ull;
-}
-
-__global__ void __launch_bounds__(kWarps * 32) k_star_a(StarA a)
-{
-    __shared__ SmemA sm_all[kWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t v64 = (int64_t)blockIdx.x * kWarps + warp;
-    if (v64 >= a.V) return;
-    const int v = (int)v64;
-    SmemA &sm = sm_all[warp];
-    const int64_t b0 = a.vt_off[v];
-    const int D = (int)(a.vt_off[v + 1] - b0);
-    if (D > kMaxStar) {
-        if (lane == 0) {
-            atomicOr(&a.st->flags, ST_HEAVY_STAR);
-            atomicMin(&a.st->bad_vertex, v);
-            a.deg[v] = 0;
-        }
-        return;
-    }
-    for (int h = lane; h < kHash; h += 32) {
-        sm.hkey[h] = -1;
-        sm.hmask[h] = 0ull;
-    }
-    load_star(sm.t, a.vt, b0, D, a.tvs, v, lane);
-    __syncwarp();
-
-    // Distinct neighbours with the star positions holding them.  Lanes that
-    // hold the same neighbour in the same column are merged by
-    // __match_any_sync first, so one lane per group touches the table.
-    bool full = false;
-    for (int base = 0; base < D; base += 32) {
-        const int i = base + lane;
-        const bool act = i < D;
-        const unsigned amask = __ballot_sync(kFull, act);
-        if (act) {
-            const int4 w = sm.t.tv[i];
-            const int s = sm.t.sv[i];
-#pragma unroll
-            for (int jj = 0; jj < 3; jj++) {
-                const int t = jj + (jj >= s);
-                const int u = get4(w, t);
-                const unsigned grp = __match_any_sync(amask, u);
-                if (lane == __ffs(grp) - 1)
-                    full |= !h_insert(sm.hkey, sm.hmask, u, (unsigned long long)grp << base);
-            }
-        }
-    }
-    __syncwarp();
-    if (__any_sync(kFull, full)) {
-        if (lane == 0) {
-            atomicOr(&a.st->flags, ST_HASH_FULL);
-            atomicMin(&a.st->bad_vertex, v);
-            a.deg[v] = 0;
-        }
-        return;
-    }
-
-    // Compact the table into the padded per-vertex summary: capacity D + 2,
-    // enough for any vertex whose link is a triangulated sphere or disk, or
-    // 3D (always enough) when a.wide is set after an overflow.
-    const int64_t sbase = a.wide ? 3 * b0 : b0 + 2 * v64;
-    const int cap = a.wide ? 3 * D : D + 2;
-    int cnt = 0;
-    for (int s0 = 0; s0 < kHash; s0 += 32) {
-        const int k = sm.hkey[s0 + lane];
-        const bool valid = k >= 0;
-        const unsigned bal = __ballot_sync(kFull, valid);
-        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-        if (valid && pos < cap) {
-            a.sum_nb[sbase + pos] = k;
-            a.sum_mask[sbase + pos] = sm.hmask[s0 + lane];
-        }
-        cnt += __popc(bal);
-    }
-    if (lane == 0) {
-        a.deg[v] = cnt <= cap ? cnt : 0;
-        if (cnt > cap) {
-            atomicOr(&a.st->flags, ST_STAR_OVERFLOW);
-            atomicMin(&a.st->bad_vertex, v);
-        }
-        if (cnt > kMaxDeg) {
-            atomicOr(&a.st->flags, ST_HEAVY_DEG);
-            atomicMax(&a.st->max_deg, cnt);
-        }
-    }
-    if (cnt > cap) return;
-
-    // First occurrences of the edges v owns (v is the low end).
-    for (int h = lane; h < kHash; h += 32) {
-        const int u = sm.hkey[h];
-        if (u > v) {
-            const unsigned long long m = sm.hmask[h];
-            const int i = __ffsll((long long)m) - 1;
-            const int4 w = sm.t.tv[i];
-            const int s = sm.t.sv[i], su = slot_of(w, u);
-            const long long p = 6LL * sm.t.cell[i] + pair_slot(min(s, su), max(s, su));
-            atomicOr(a.eflag + (p >> 5), 1u << (p & 31));
-        }
-    }
-    // First occurrences of the faces v owns: in a cell where v sits in slot
-    // 0 it is the low vertex of the faces omitting slots 1, 2, 3; in slot 1,
-    // of the face omitting slot 0.
-    for (int i = lane; i < D; i += 32) {
-        const int s = sm.t.sv[i];
-        if (s > 1) continue;
-        const int4 w = sm.t.tv[i];
-        const int o_lo = (s == 0) ? 1 : 0, o_hi = (s == 0) ? 3 : 0;
-        for (int o = o_lo; o <= o_hi; o++) {
-            int x = -1, y = -1;
-#pragma unroll
-            for (int t = 0; t < 4; t++)
-                if (t != s && t != o) {
-                    if (x < 0) x = get4(w, t); else y = get4(w, t);
-                }
-            const unsigned long long m = h_lookup(sm.hkey, sm.hmask, x) & h_lookup(sm.hkey, sm.hmask, y);
-            if (__popcll(m) > 2) {
-                atomicOr(&a.st->flags, ST_NONMANIFOLD_FACE);
-                atomicMin(&a.st->bad_cell, sm.t.cell[i]);
-            }
-            if (__ffsll((long long)m) - 1 == i) {
-                const long long q = 4LL * sm.t.cell[i] + (3 - o);
-                atomicOr(a.fflag + (q >> 5), 1u << (q & 31));
-            }
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256)
-k_vv_finalize(const int64_t *__restrict__ vt_off, const int *__restrict__ sum_nb,
-              const unsigned long long *__restrict__ sum_mask, const int64_t *__restrict__ vv_off,
-              int64_t V, int wide, int *__restrict__ vv, unsigned long long *__restrict__ vvmask)
-{
-    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
-    const int64_t sb = wide ? 3 * vt_off[v] : vt_off[v] + 2 * v;
-    const int64_t ob = vv_off[v];
-    const int n = (int)(vv_off[v + 1] - ob);
-    for (int k = 0; k < n; k++) {
-        const int x = sum_nb[sb + k];
-        const unsigned long long mx = sum_mask[sb + k];
-        int j = k - 1;
-        while (j >= 0 && vv[ob + j] > x) {
-            vv[ob + j + 1] = vv[ob + j];
-            vvmask[ob + j + 1] = vvmask[ob + j];
-            j--;
-        }
-        vv[ob + j + 1] = x;
-        vvmask[ob + j + 1] = mx;
-    }
-}
-
-struct SmemB {
-    StarTile t;
-    int nb[kMaxDeg];
-    unsigned long long nmask[kMaxDeg];
-    int nid[kMaxDeg];
-};
-
-// Load star + sorted neighbours (+ edge ids when eidv is given).
-__device__ __forceinline__ bool load_vertex(SmemB &sm, int v, int lane, const int64_t *vt_off,
-                                            const int *vt, const int4 *tvs, const int64_t *vv_off,
-                                            const int *vv, const unsigned long long *vvmask,
-                                            const int *eidv, int &D, int &deg, int64_t &vb)
-{
-    const int64_t b0 = vt_off[v];
-    D = (int)(vt_off[v + 1] - b0);
-    vb = vv_off[v];
-    deg = (int)(vv_off[v + 1] - vb);
-    if (D > kMaxStar || deg > kMaxDeg) return false;
-    load_star(sm.t, vt, b0, D, tvs, v, lane);
-    for (int k = lane; k < deg; k += 32) {
-        sm.nb[k] = __ldg(vv + vb + k);
-        sm.nmask[k] = __ldg(vvmask + vb + k);
-        if (eidv) sm.nid[k] = __ldg(eidv + vb + k);
-    }
-    __syncwarp();
-    return true;
-}
-
-__global__ void __launch_bounds__(kWarps * 32) k_star_b(StarB b)
-{
-    __shared__ SmemB sm_all[kWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t v64 = (int64_t)blockIdx.x * kWarps + warp;
-    if (v64 >= b.V) return;
-    const int v = (int)v64;
-    SmemB &sm = sm_all[warp];
-    int D, deg;
-    int64_t vb;
-    if (!load_vertex(sm, v, lane, b.vt_off, b.vt, b.tvs, b.vv_off, b.vv,
-                     reinterpret_cast<const unsigned long long *>(b.vvmask), nullptr, D, deg, vb))
-        return;
-
-    // 1. id of every incident edge (first occurrence -> rank)
-    for (int k = lane; k < deg; k += 32) {
-        const int u = sm.nb[k];
-        const unsigned long long m = sm.nmask[k];
-        const int i = __ffsll((long long)m) - 1;
-        const int4 w = sm.t.tv[i];
-        const int s = sm.t.sv[i], su = slot_of(w, u);
-        const long long p = 6LL * sm.t.cell[i] + pair_slot(min(s, su), max(s, su));
-        const int id = bit_rank(b.eflag, b.epre, p);
-        sm.nid[k] = id;
-        b.eidv[vb + k] = id;
-        if (u > v) {
-            if (b.ev) reinterpret_cast<int2 *>(b.ev)[id] = make_int2(v, u);
-            if (b.et_cnt) b.et_cnt[id] = __popcll(m);
-            if (b.ef_cnt) {
-                int c = 0;
-                for (int kk = 0; kk < deg; kk++) c += (kk != k) && (sm.nmask[kk] & m);
-                b.ef_cnt[id] = c;
-            }
-            if (b.ee_cnt) b.ee_cnt[id] = deg + (int)(b.vv_off[u + 1] - b.vv_off[u]) - 2;
-        }
-    }
-    __syncwarp();
-
-    // 2. TE entries of the pairs whose low end is v
-    if (b.te) {
-        for (int i = lane; i < D; i += 32) {
-            const int s = sm.t.sv[i];
-            const int4 w = sm.t.tv[i];
-            int *row = b.te + 6LL * sm.t.cell[i];
-            for (int t = s + 1; t < 4; t++) {
-                const int k = lower_bound_sm(sm.nb, deg, get4(w, t));
-                row[pair_slot(s, t)] = sm.nid[k];
-            }
-        }
-    }
-
-    // 3. faces v owns: TF entries of every occurrence; FV, FT and counts once
-    const bool faces = b.tf || b.fv || b.ft || b.ff_cnt || b.tt_cnt;
-    if (faces) {
-        for (int i = lane; i < D; i += 32) {
-            const int s = sm.t.sv[i];
-            if (s > 1) continue;
-            const int4 w = sm.t.tv[i];
-            const int c = sm.t.cell[i];
-            const int o_lo = (s == 0) ? 1 : 0, o_hi = (s == 0) ? 3 : 0;
-            for (int o = o_lo; o <= o_hi; o++) {
-                int x = -1, y = -1;
-#pragma unroll
-                for (int t = 0; t < 4; t++)
-                    if (t != s && t != o) {
-                        if (x < 0) x = get4(w, t); else y = get4(w, t);
-                    }
-                const int kx = lower_bound_sm(sm.nb, deg, x), ky = lower_bound_sm(sm.nb, deg, y);
-                const unsigned long long m = sm.nmask[kx] & sm.nmask[ky];
-                const int f = __ffsll((long long)m) - 1;
-                const int of = (f == i) ? o : omitted_slot(sm.t.tv[f], v, x, y);
-                const long long q = 4LL * sm.t.cell[f] + (3 - of);
-                const int fid = bit_rank(b.fflag, b.fpre, q);
-                if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                if (f == i) {
-                    const unsigned long long m2 = m & (m - 1);
-                    const int c2 = m2 ? sm.t.cell[__ffsll((long long)m2) - 1] : -1;
-                    if (b.fv) {
-                        b.fv[3LL * fid] = v;
-                        b.fv[3LL * fid + 1] = x;
-                        b.fv[3LL * fid + 2] = y;
-                    }
-                    if (b.ft) reinterpret_cast<int2 *>(b.ft)[fid] = make_int2(c, c2);
-                    if (b.ff_cnt) b.ff_cnt[fid] = 3 * __popcll(m);
-                    if (b.tt_cnt && c2 >= 0) {
-                        atomicAdd(b.tt_cnt + c, 1);
-                        atomicAdd(b.tt_cnt + c2, 1);
-                    }
-                }
-            }
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kWarps * 32) k_star_c(StarC p)
-{
-    __shared__ SmemB sm_all[kWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t v64 = (int64_t)blockIdx.x * kWarps + warp;
-    if (v64 >= p.V) return;
-    const int v = (int)v64;
-    SmemB &sm = sm_all[warp];
-    int D, deg;
-    int64_t vb;
-    if (!load_vertex(sm, v, lane, p.vt_off, p.vt, p.tvs, p.vv_off, p.vv,
-                     reinterpret_cast<const unsigned long long *>(p.vvmask), p.eidv, D, deg, vb))
-        return;
-    for (int k = lane; k < deg; k += 32) {
-        const int u = sm.nb[k];
-        if (u <= v) continue;
-        const int id = sm.nid[k];
-        const unsigned long long m = sm.nmask[k];
-        if (p.et) {
-            int64_t pos = p.et_off[id];
-            unsigned long long mm = m;
-            while (mm) {
-                const int i = __ffsll((long long)mm) - 1;
-                mm &= mm - 1;
-                p.et[pos++] = sm.t.cell[i];
-            }
-        }
-        if (p.ef) {
-            const int64_t pos0 = p.ef_off[id];
-            int n = 0;
-            for (int kk = 0; kk < deg; kk++) {
-                if (kk == k) continue;
-                const unsigned long long mm = m & sm.nmask[kk];
-                if (!mm) continue;
-                const int f = __ffsll((long long)mm) - 1;
-                const int of = omitted_slot(sm.t.tv[f], v, u, sm.nb[kk]);
-                const long long q = 4LL * sm.t.cell[f] + (3 - of);
-                const int fid = bit_rank(p.fflag, p.fpre, q);
-                int64_t j = pos0 + n - 1;
-                while (j >= pos0 && p.ef[j] > fid) {
-                    p.ef[j + 1] = p.ef[j];
-                    j--;
-                }
-                p.ef[j + 1] = fid;
-                n++;
-            }
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Cell, face and edge fills
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int rank_of(const uint2 *__restrict__ rk, long long p)
+{
+    const uint2 w = __ldg(rk + (p >> 5));
+    return (int)w.y + __popc(w.x & ((1u << (p & 31)) - 1u));
+}
+
+// FE of each face at its first cell (FT[f][0] == c); TT rows at offset
+// 4c - (boundary faces in cells before c), since a cell's TT row holds one
+// entry per interior face; the closing offsets of TT and FF.
 __global__ void __launch_bounds__(256)
-k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, const int *__restrict__ te,
-             const int *__restrict__ tf, const int *__restrict__ ft, int *__restrict__ fe,
-             const int64_t *__restrict__ tt_off, int *__restrict__ tt)
+k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__restrict__ te,
+             const int *__restrict__ tf, const int *__restrict__ ft, const uint2 *__restrict__ brank,
+             int *__restrict__ fe, int64_t *__restrict__ tt_off, int *__restrict__ tt,
+             int64_t *__restrict__ ff_off)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
+    if (c == T - 1) {
+        const int64_t nb = rank_of(brank, 4 * T);
+        if (tt_off) tt_off[T] = 4 * T - nb;
+        if (ff_off) ff_off[F] = 3 * (2 * F - nb);
+    }
     const int4 f4 = reinterpret_cast<const int4 *>(tf)[c];
     int nbr[4];
     int n = 0;
@@ -581,7 +209,9 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, const int *__restrict__ te
             while (j >= 0 && nbr[j] > x) { nbr[j + 1] = nbr[j]; j--; }
             nbr[j + 1] = x;
         }
-        int *row = tt + tt_off[c];
+        const int64_t off = 4 * c - rank_of(brank, 4 * c);
+        tt_off[c] = off;
+        int *row = tt + off;
         for (int i = 0; i < n; i++) row[i] = nbr[i];
     }
 }
@@ -615,25 +245,66 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
     for (int i = 0; i < n; i++) row[i] = r[i];
 }
 
-__global__ void __launch_bounds__(256)
+// EE: a block takes 64 consecutive edges; thread (edge, side) stages the
+// sorted incident-edge row of one endpoint in shared memory, then places each
+// element at its rank in the merged row: an element x of one row has k
+// smaller elements in its own row and lower_bound(x) in the other; both rows
+// hold e itself once (and share nothing else), so its slot in e's EE row is
+// k + lower_bound - 2 * (e < x).
+constexpr int kEeEdges = 64;
+
+__device__ __forceinline__ int lower_bound_s(const int *a, int n, int key)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        if (a[m] < key) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(2 * kEeEdges)
 k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_off,
           const int *__restrict__ eid, const int64_t *__restrict__ ee_off, int *__restrict__ ee)
 {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int rows[2 * kEeEdges][kMaxDeg];
+    __shared__ int len[2 * kEeEdges];
+    __shared__ long long start[2 * kEeEdges];
+    const int64_t e0 = (int64_t)blockIdx.x * kEeEdges;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // where the rows are: one thread per (edge, side), all in flight at once
+    {
+        const int r = threadIdx.x;
+        const int64_t e = e0 + (r >> 1);
+        int n = 0;
+        long long b = 0;
+        if (e < E) {
+            const int v = __ldg(ev + 2 * e + (r & 1));
+            b = __ldg(vv_off + v);
+            n = (int)(__ldg(vv_off + v + 1) - b);
+        }
+        start[r] = b;
+        len[r] = n;
+    }
+    __syncthreads();
+    // copy: each warp moves 32 rows, lanes along a row (coalesced)
+#pragma unroll 4
+    for (int r = warp * 32; r < warp * 32 + 32; r++) {
+        const int n = len[r];
+        const long long b = start[r];
+        for (int k = lane; k < n; k += 32) rows[r][k] = __ldg(eid + b + k);
+    }
+    __syncthreads();
+    const int r = threadIdx.x;
+    const int64_t e = e0 + (r >> 1);
     if (e >= E) return;
-    const int2 ab = reinterpret_cast<const int2 *>(ev)[e];
-    const int *A = eid + vv_off[ab.x];
-    const int *B = eid + vv_off[ab.y];
-    const int na = (int)(vv_off[ab.x + 1] - vv_off[ab.x]);
-    const int nb = (int)(vv_off[ab.y + 1] - vv_off[ab.y]);
+    const int *mine = rows[r], *other = rows[r ^ 1];
+    const int nm = len[r], no = len[r ^ 1];
     int *out = ee + ee_off[e];
-    int i = 0, j = 0, p = 0;
-    while (i < na || j < nb) {
-        int x;
-        if (j >= nb || (i < na && A[i] < B[j])) x = A[i++];
-        else if (i >= na || B[j] < A[i]) x = B[j++];
-        else { x = A[i++]; j++; }
-        if (x != (int)e) out[p++] = x;
+    for (int k = 0; k < nm; k++) {
+        const int x = mine[k];
+        if (x == (int)e) continue;
+        out[k + lower_bound_s(other, no, x) - 2 * ((int)e < x)] = x;
     }
 }
 
@@ -674,6 +345,15 @@ k_tt_vertex(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__
     if (!FILL) cnt[c] = n;
 }
 
+__global__ void k_reset_status(DevStatus *st)
+{
+    st->flags = 0;
+    st->bad_cell = INT_MAX;
+    st->bad_vertex = INT_MAX;
+    st->max_star = 0;
+    st->max_deg = 0;
+}
+
 inline unsigned blocks_for(int64_t n, int threads)
 {
     return (unsigned)((n + threads - 1) / threads);
@@ -684,6 +364,12 @@ inline unsigned blocks_for(int64_t n, int threads)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+void launch_reset_status(DevStatus *st, cudaStream_t s)
+{
+    Launch L("k_reset_status", s);
+    k_reset_status<<<1, 1, 0, s>>>(st);
+}
+
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
                   DevStatus *st, cudaStream_t s)
 {
@@ -714,54 +400,19 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
     }
 }
 
-void launch_star_a(const StarA &a, cudaStream_t s)
-{
-    if (a.V == 0) return;
-    {
-        Launch L("k_star_a", s);
-        k_star_a<<<blocks_for(a.V, kWarps), kWarps * 32, 0, s>>>(a);
-    }
-}
 
-void launch_vv_finalize(const int64_t *vt_off, const int32_t *sum_nb, const uint64_t *sum_mask,
-                        const int64_t *vv_off, int64_t V, int wide, int32_t *vv, uint64_t *vvmask,
-                        cudaStream_t s)
-{
-    if (V == 0) return;
-    {
-        Launch L("k_vv_finalize", s);
-        k_vv_finalize<<<blocks_for(V, 256), 256, 0, s>>>(
-            vt_off, sum_nb, reinterpret_cast<const unsigned long long *>(sum_mask), vv_off, V, wide, vv,
-            reinterpret_cast<unsigned long long *>(vvmask));
-    }
-}
 
-void launch_star_b(const StarB &b, cudaStream_t s)
-{
-    if (b.V == 0) return;
-    {
-        Launch L("k_star_b", s);
-        k_star_b<<<blocks_for(b.V, kWarps), kWarps * 32, 0, s>>>(b);
-    }
-}
 
-void launch_star_c(const StarC &c, cudaStream_t s)
-{
-    if (c.V == 0) return;
-    {
-        Launch L("k_star_c", s);
-        k_star_c<<<blocks_for(c.V, kWarps), kWarps * 32, 0, s>>>(c);
-    }
-}
 
-void launch_cell_fe_tt(const int4 *tvs, int64_t T, const int32_t *te, const int32_t *tf,
-                       const int32_t *ft, int32_t *fe, const int64_t *tt_off, int32_t *tt,
-                       cudaStream_t s)
+void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
+                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fe,
+                       int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s)
 {
     if (T == 0) return;
     {
         Launch L("k_cell_fe_tt", s);
-        k_cell_fe_tt<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, te, tf, ft, fe, tt_off, tt);
+        k_cell_fe_tt<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, F, te, tf, ft, brank, fe, tt_off,
+                                                         tt, ff_off);
     }
 }
 
@@ -781,7 +432,8 @@ void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const i
     if (E == 0) return;
     {
         Launch L("k_ee_fill", s);
-        k_ee_fill<<<blocks_for(E, 256), 256, 0, s>>>(ev, E, vv_off, eid_sorted, ee_off, ee);
+        k_ee_fill<<<blocks_for(E, kEeEdges), 2 * kEeEdges, 0, s>>>(ev, E, vv_off, eid_sorted,
+                                                                   ee_off, ee);
     }
 }
 

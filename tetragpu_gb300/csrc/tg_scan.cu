@@ -23,13 +23,18 @@ struct ScanParams {
 __device__ __forceinline__ int64_t load_value(const ScanJob &j, int64_t i)
 {
     if (j.kind == SCAN_COUNT_I32) return (int64_t)__ldg((const int32_t *)j.in + i);
+    if (j.kind == SCAN_SQUARE_I32) {
+        const int64_t x = __ldg((const int32_t *)j.in + i);
+        return x * x;
+    }
     return (int64_t)__popc(__ldg((const uint32_t *)j.in + i));
 }
 
 __device__ __forceinline__ void store_value(const ScanJob &j, int64_t i, int64_t v)
 {
-    if (j.kind == SCAN_COUNT_I32) ((int64_t *)j.out)[i] = v;
-    else ((int32_t *)j.out)[i] = (int32_t)v;
+    if (j.kind != SCAN_POPC_RANK) ((int64_t *)j.out)[i] = v;
+    else ((uint2 *)j.out)[i] = make_uint2(i < j.n ? __ldg((const uint32_t *)j.in + i) : 0u,
+                                          (unsigned)v);
 }
 
 // Block-wide exclusive scan of one int64 per thread; returns the block total.

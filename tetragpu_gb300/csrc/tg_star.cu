@@ -1,0 +1,747 @@
+// tg_star.cu -- the per-vertex "star" passes of the relation pipeline.
+//
+// The star of a vertex v is its VT row: the cells around v, ascending.  Every
+// cell that holds an edge or a face at v is in it, so within the star
+//   * the first position holding a neighbour u is the first occurrence of
+//     edge (v,u) in the reference's cell-order scan, and
+//   * the first position holding both x and y is the first occurrence of
+//     face (v,x,y),
+// which is what the reference CPU ids are ranks of (src/cpu_extraction.cpp:
+// 28-62 edges, 122-174 faces).
+//
+// Work decomposition: VT is cut into windows of kWin entries.  A block owns
+// the vertices whose rows START in its window (at most kWin + kMaxStar - 1
+// entries), stages their cells and the cells' sorted TV rows in shared
+// memory (all gathers in flight at once), and gives one thread to each
+// (vertex, star cell) entry.  A shared-memory hash keyed by (vertex,
+// neighbour) holds, per neighbour, the 64-bit mask of star positions whose
+// cell contains it; lanes holding the same key are merged by
+// __match_any_sync first, so one lane per group touches the table.  With the
+// masks, "first position holding u" is a count-trailing-zeros and "first
+// position holding x and y" a ctz of an AND.
+//
+//   k_star_a  first-occurrence bitmaps (edges owned by v = v is the low end,
+//             faces owned by v = v is the lowest vertex, boundary faces), the
+//             ET / EF row lengths at each owned edge's first-occurrence slot,
+//             and neighbour counts
+//   k_star_b  ids (ranks of first occurrences), sorted VV rows, incident edge
+//             ids (by neighbour and by id), EV, TE, TF, FV, FT, FF offsets,
+//             ET and EF rows
+#include "tg_internal.h"
+
+namespace tg {
+namespace {
+
+constexpr int kWin = 256;                 // VT entries per block window
+constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in the window)
+constexpr int kThreads = 256;
+constexpr int kHash = 1024;               // (vertex, neighbour) slots per block
+constexpr unsigned long long kEmpty = ~0ull;
+
+__device__ __forceinline__ int get4(const int4 &w, int i)
+{
+    return i == 0 ? w.x : (i == 1 ? w.y : (i == 2 ? w.z : w.w));
+}
+__device__ __forceinline__ int slot_of(const int4 &w, int u)
+{
+    return (w.x < u) + (w.y < u) + (w.z < u) + (w.w < u);
+}
+__device__ __forceinline__ int pair_slot(int s, int t)  // s < t, reference TE order
+{
+    return s == 0 ? t - 1 : (s == 1 ? t + 1 : 5);
+}
+__device__ __forceinline__ int omitted_slot(const int4 &w, int a, int b, int c)
+{
+    if (w.x != a && w.x != b && w.x != c) return 0;
+    if (w.y != a && w.y != b && w.y != c) return 1;
+    if (w.z != a && w.z != b && w.z != c) return 2;
+    return 3;
+}
+// id of occurrence p: the set bits of the first-occurrence bitmap below p
+__device__ __forceinline__ int rank_of(const uint2 *__restrict__ rk, long long p)
+{
+    const uint2 w = __ldg(rk + (p >> 5));
+    return (int)w.y + __popc(w.x & ((1u << (p & 31)) - 1u));
+}
+__device__ __forceinline__ int ctz64(unsigned long long m) { return __ffsll((long long)m) - 1; }
+
+struct Stage {
+    int cell[kCap];
+    int4 tv[kCap];
+    int vid[kCap];
+    int meta[kCap];                     // row start | D << 10 | slot of v << 20
+    unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
+    unsigned long long hmask[kHash];    // star positions whose cell holds the neighbour
+    int hval[kHash];                    // pass B: edge id of (v, neighbour)
+    short cslot[kCap][4];               // hash slot of each entry's 3 candidates (other vertices)
+    int cnt[kCap];                      // per row start: neighbours listed so far
+    int list[3 * kCap];                 // per row start rs: its neighbours' hash slots at 3*rs..
+    int n, vlo, vhi, full;
+    long long base;
+};
+
+__device__ __forceinline__ int m_rs(int m) { return m & 1023; }
+__device__ __forceinline__ int m_D(int m) { return (m >> 10) & 1023; }
+__device__ __forceinline__ int m_sv(int m) { return (m >> 20) & 3; }
+
+__device__ __forceinline__ int64_t lower_bound_g(const int64_t *a, int64_t n, int64_t key)
+{
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t m = (lo + hi) >> 1;
+        if (a[m] < key) lo = m + 1; else hi = m;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ unsigned hslot(unsigned long long key)
+{
+    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - 10));
+}
+
+__device__ __forceinline__ int h_insert(Stage &S, unsigned long long key, unsigned long long bits)
+{
+    unsigned h = hslot(key);
+    for (int probe = 0; probe < kHash; probe++) {
+        const unsigned long long old = atomicCAS(&S.hkey[h], kEmpty, key);
+        if (old == kEmpty || old == key) {
+            atomicOr(&S.hmask[h], bits);
+            return (int)h;
+        }
+        h = (h + 1) & (kHash - 1);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ unsigned long long hk(int rs, int u)
+{
+    return ((unsigned long long)(unsigned)rs << 32) | (unsigned)u;
+}
+
+// Stage the block's window and fill the (vertex, neighbour) table.  Returns
+// false (block-uniformly) when the window cannot be handled here.  win[b] is
+// the first vertex whose row starts at or after entry kWin * b.
+__device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ vt_off,
+                               const int *__restrict__ win, const int *__restrict__ vt,
+                               const int4 *__restrict__ tvs, DevStatus *st, int *deg_zero)
+{
+    if (threadIdx.x == 0) {
+        const int vlo = win[blockIdx.x], vhi = win[blockIdx.x + 1];
+        S.vlo = vlo;
+        S.vhi = vhi;
+        S.base = vt_off[vlo];
+        S.n = (int)(vt_off[vhi] - S.base);
+        S.full = 0;
+    }
+    for (int h = threadIdx.x; h < kHash; h += blockDim.x) {
+        S.hkey[h] = kEmpty;
+        S.hmask[h] = 0ull;
+    }
+    __syncthreads();
+    const int n = S.n;
+    if (n > kCap) {
+        if (threadIdx.x == 0) {
+            atomicOr(&st->flags, ST_HEAVY_STAR);
+            atomicMin(&st->bad_vertex, S.vlo);
+        }
+        return false;
+    }
+    const long long base = S.base;
+    for (int v = S.vlo + threadIdx.x; v < S.vhi; v += blockDim.x) {
+        const int rs = (int)(vt_off[v] - base);
+        const int D = (int)(vt_off[v + 1] - vt_off[v]);
+        if (D == 0 && deg_zero) deg_zero[v] = 0;
+        if (D > kMaxStar) {
+            atomicOr(&st->flags, ST_HEAVY_STAR);
+            atomicMin(&st->bad_vertex, v);
+            S.full = 1;
+        }
+        for (int i = 0; i < D; i++) {
+            S.vid[rs + i] = v;
+            S.meta[rs + i] = rs | (D << 10);
+        }
+        if (D > 0) S.cnt[rs] = 0;
+    }
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = __ldg(vt + base + e);
+        S.cell[e] = c;
+        S.tv[e] = __ldg(tvs + c);
+    }
+    __syncthreads();
+    if (S.full) return false;
+    // insert the 3 other vertices of every staged cell, keyed by the row
+    for (int e0 = 0; e0 < n; e0 += blockDim.x) {
+        const int e = e0 + threadIdx.x;
+        const bool act = e < n;
+        const unsigned amask = __ballot_sync(0xffffffffu, act);
+        if (!act) continue;
+        const int v = S.vid[e];
+        const int m = S.meta[e];
+        const int rs = m_rs(m);
+        const int4 w = S.tv[e];
+        const int sv = slot_of(w, v);
+        S.meta[e] = m | (sv << 20);
+        const int ewarp = e - (threadIdx.x & 31);  // entry of lane 0 of this warp
+        const int shift = ewarp - rs;               // lane l sits at row position l + shift
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int t = k + (k >= sv);
+            const unsigned long long key = hk(rs, get4(w, t));
+            const unsigned grp = __match_any_sync(amask, key);
+            const int leader = __ffs(grp) - 1;
+            int h = 0;
+            if ((int)(threadIdx.x & 31) == leader) {
+                const unsigned long long bits =
+                    shift >= 0 ? (unsigned long long)grp << shift : (unsigned long long)grp >> -shift;
+                h = h_insert(S, key, bits);
+                if (h < 0) {
+                    S.full = 1;
+                    h = 0;
+                }
+            }
+            S.cslot[e][k] = (short)__shfl_sync(amask, h, leader);
+        }
+    }
+    __syncthreads();
+    if (S.full) {
+        if (threadIdx.x == 0) {
+            atomicOr(&st->flags, ST_HASH_FULL);
+            atomicMin(&st->bad_vertex, S.vlo);
+        }
+        return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void set_bit(uint32_t *bits, long long p)
+{
+    atomicOr(bits + (p >> 5), 1u << (p & 31));
+}
+
+// candidate index (0..2) of slot t in a cell where v sits in slot sv (t != sv)
+__device__ __forceinline__ int cand_of(int t, int sv) { return t - (t > sv); }
+
+// The two vertices of a face owned by the vertex in slot sv with slot o omitted.
+__device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x, int &y)
+{
+    x = -1;
+    y = -1;
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+        if (t != sv && t != o) {
+            if (x < 0) x = get4(w, t); else y = get4(w, t);
+        }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
+{
+    __shared__ Stage S;
+    if (!stage_and_hash(S, a.vt_off, a.win, a.vt, a.tvs, a.st, a.deg)) return;
+    const int n = S.n;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int v = S.vid[e], m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        const int4 w = S.tv[e];
+        const int c = S.cell[e];
+        unsigned long long cm[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) cm[k] = S.hmask[S.cslot[e][k]];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int t = k + (k >= sv);
+            const int u = get4(w, t);
+            const unsigned long long mu = cm[k];
+            if (ctz64(mu) != pos) continue;                     // not the first sighting
+            atomicAdd(&S.cnt[rs], 1);
+            if (u <= v) continue;
+            // an edge v owns: flag its first occurrence, record its ET and EF
+            // row lengths at that occurrence slot.  A face (v,u,x) is counted
+            // in the first cell holding u and x.
+            const long long p = 6LL * c + pair_slot(sv, t);
+            set_bit(a.eflag, p);
+            int n_ef = 0;
+            for (unsigned long long mm = mu; mm; mm &= mm - 1) {
+                const int j = ctz64(mm);
+                const int ej = rs + j;
+                const int4 wj = S.tv[ej];
+                const int sj = m_sv(S.meta[ej]);
+                const int ku = cand_of(slot_of(wj, u), sj);
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk == ku) continue;
+                    n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
+                }
+            }
+            a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+        }
+        if (sv <= 1) {
+            // faces whose lowest vertex is v: omit slot 1, 2, 3 when v is in
+            // slot 0; omit slot 0 when v is in slot 1.  The face's other two
+            // vertices are two of this entry's candidates.
+            const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
+            for (int o = o_lo; o <= o_hi; o++) {
+                const int ko = cand_of(o, sv);      // the omitted candidate
+                const unsigned long long mf = ko == 0 ? cm[1] & cm[2] : (ko == 1 ? cm[0] & cm[2] : cm[0] & cm[1]);
+                if (ctz64(mf) != pos) continue;
+                const long long q = 4LL * c + (3 - o);
+                set_bit(a.fflag, q);
+                const int ncell = __popcll(mf);
+                if (ncell == 1) set_bit(a.fbnd, q);
+                if (ncell > 2) {
+                    atomicOr(&a.st->flags, ST_NONMANIFOLD_FACE);
+                    atomicMin(&a.st->bad_cell, c);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int m = S.meta[e];
+        if (m_rs(m) != e) continue;
+        const int d = S.cnt[e];
+        a.deg[S.vid[e]] = d;
+        if (d > kMaxDeg) {
+            atomicOr(&a.st->flags, ST_HEAVY_DEG);
+            atomicMax(&a.st->max_deg, d);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
+{
+    __shared__ Stage S;
+    if (!stage_and_hash(S, b.vt_off, b.win, b.vt, b.tvs, b.st, nullptr)) return;
+    const int n = S.n;
+
+    // 1. list every vertex's neighbours (the hash slot of each first sighting)
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int rs = m_rs(S.meta[e]), pos = e - rs;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int h = S.cslot[e][k];
+            if (ctz64(S.hmask[h]) == pos) S.list[3 * rs + atomicAdd(&S.cnt[rs], 1)] = h;
+        }
+    }
+    __syncthreads();
+
+    // 2. per first sighting: edge id, VV position; for owned edges EV, ET, EF
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int v = S.vid[e], m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        const int4 w = S.tv[e];
+        const int c = S.cell[e];
+        const int deg = S.cnt[rs];
+        const long long vvo = b.vv_off[v];
+#pragma unroll 1
+        for (int k = 0; k < 3; k++) {
+            const int h = S.cslot[e][k];
+            const unsigned long long mu = S.hmask[h];
+            if (ctz64(mu) != pos) continue;
+            const int t = k + (k >= sv);
+            const int u = get4(w, t);
+            int rank = 0;
+            for (int i = 0; i < deg; i++) rank += (int)(unsigned)S.hkey[S.list[3 * rs + i]] < u;
+            const int id = rank_of(b.erank, 6LL * c + pair_slot(min(sv, t), max(sv, t)));
+            S.hval[h] = id;
+            b.vv[vvo + rank] = u;
+            b.eidv[vvo + rank] = id;
+            if (u <= v) continue;
+            if (b.ev) reinterpret_cast<int2 *>(b.ev)[id] = make_int2(v, u);
+            if (b.et) {
+                long long p = b.et_off[id];
+                for (unsigned long long mm = mu; mm; mm &= mm - 1) b.et[p++] = S.cell[rs + ctz64(mm)];
+            }
+            if (b.ef) {
+                const long long p0 = b.ef_off[id];
+                int cnt = 0;
+                for (unsigned long long mm = mu; mm; mm &= mm - 1) {
+                    const int j = ctz64(mm);
+                    const int ej = rs + j;
+                    const int4 wj = S.tv[ej];
+                    const int sj = m_sv(S.meta[ej]);
+                    const int ku = cand_of(slot_of(wj, u), sj);
+#pragma unroll
+                    for (int kk = 0; kk < 3; kk++) {
+                        if (kk == ku) continue;
+                        if (ctz64(mu & S.hmask[S.cslot[ej][kk]]) != j) continue;
+                        const int tx = kk + (kk >= sj);
+                        // the face (v,u,x) omits the slot of cell j that is
+                        // neither v, u nor x: 6 - sj - su - tx
+                        const int of = 6 - sj - slot_of(wj, u) - tx;
+                        const int fid = rank_of(b.frank, 4LL * S.cell[ej] + (3 - of));
+                        long long i = p0 + cnt - 1;
+                        while (i >= p0 && b.ef[i] > fid) {
+                            b.ef[i + 1] = b.ef[i];
+                            i--;
+                        }
+                        b.ef[i + 1] = fid;
+                        cnt++;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // 3. incident edge ids by id (for EE), TE entries of the pairs v is the
+    //    low end of, and the faces v owns
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int v = S.vid[e], m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        const int4 w = S.tv[e];
+        const int c = S.cell[e];
+        if (b.eid_sorted) {
+            const int deg = S.cnt[rs];
+            const long long vvo = b.vv_off[v];
+            for (int k = 0; k < 3; k++) {
+                const int h = S.cslot[e][k];
+                if (ctz64(S.hmask[h]) != pos) continue;
+                const int id = S.hval[h];
+                int r = 0;
+                for (int i = 0; i < deg; i++) r += S.hval[S.list[3 * rs + i]] < id;
+                b.eid_sorted[vvo + r] = id;
+            }
+        }
+        if (b.te) {
+            for (int t = sv + 1; t < 4; t++)
+                b.te[6LL * c + pair_slot(sv, t)] = S.hval[S.cslot[e][cand_of(t, sv)]];
+        }
+        if (sv <= 1 && (b.tf || b.fv || b.ft || b.ff_off)) {
+            const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
+            for (int o = o_lo; o <= o_hi; o++) {
+                int x, y;
+                face_others(w, sv, o, x, y);
+                const int ko = cand_of(o, sv);
+                const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
+                const unsigned long long mf =
+                    S.hmask[S.cslot[e][ka]] & S.hmask[S.cslot[e][kb]];
+                const int j1 = ctz64(mf);
+                const int of = (j1 == pos) ? o : omitted_slot(S.tv[rs + j1], v, x, y);
+                const long long q = 4LL * S.cell[rs + j1] + (3 - of);
+                const int fid = rank_of(b.frank, q);
+                if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
+                if (j1 != pos) continue;
+                const unsigned long long m2 = mf & (mf - 1);
+                const int c2 = m2 ? S.cell[rs + ctz64(m2)] : -1;
+                if (b.fv) {
+                    b.fv[3LL * fid] = v;
+                    b.fv[3LL * fid + 1] = x;
+                    b.fv[3LL * fid + 2] = y;
+                }
+                if (b.ft) reinterpret_cast<int2 *>(b.ft)[fid] = make_int2(c, c2);
+                // a face's FF row holds 3 entries per cell of the face, so its
+                // offset is 3 * (2 fid - boundary faces before it)
+                if (b.ff_off) b.ff_off[fid] = 3LL * (2LL * fid - rank_of(b.brank, q));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sort every VT row ascending.  Rows starting in a window are staged in
+// shared memory and each entry lands at its rank in its row (cells in a row
+// are distinct); windows holding more than kCap entries fall back to an
+// insertion sort per row in global memory.
+__global__ void __launch_bounds__(kThreads)
+k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt)
+{
+    __shared__ int cell[kCap], out[kCap], meta[kCap];
+    __shared__ int s_vlo, s_vhi, s_n;
+    __shared__ long long s_base;
+    if (threadIdx.x == 0) {
+        const int vlo = win[blockIdx.x], vhi = win[blockIdx.x + 1];
+        s_vlo = vlo;
+        s_vhi = vhi;
+        s_base = vt_off[vlo];
+        s_n = (int)(vt_off[vhi] - s_base);
+    }
+    __syncthreads();
+    const int n = s_n;
+    const long long base = s_base;
+    if (n > kCap) {
+        for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
+            const int64_t b = vt_off[v], e = vt_off[v + 1];
+            for (int64_t i = b + 1; i < e; i++) {
+                const int x = vt[i];
+                int64_t j = i - 1;
+                while (j >= b && vt[j] > x) {
+                    vt[j + 1] = vt[j];
+                    j--;
+                }
+                vt[j + 1] = x;
+            }
+        }
+        return;
+    }
+    for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
+        const int rs = (int)(vt_off[v] - base);
+        const int D = (int)(vt_off[v + 1] - vt_off[v]);
+        for (int i = 0; i < D; i++) meta[rs + i] = rs | (D << 10);
+    }
+    for (int e = threadIdx.x; e < n; e += blockDim.x) cell[e] = vt[base + e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int m = meta[e], rs = m_rs(m), D = m_D(m), x = cell[e];
+        int r = 0;
+        for (int j = rs; j < rs + D; j++) r += cell[j] < x;
+        out[rs + r] = x;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) vt[base + e] = out[e];
+}
+
+// ---------------------------------------------------------------------------
+// ET / EF / EE offsets in edge-id order.  Edge ids are ranks of first
+// occurrences, so scanning the 6T edge-occurrence slots in order visits the
+// edges in id order: a slot holding a first occurrence contributes the ET
+// and EF row lengths k_star_a left there and deg(a) + deg(b) - 2 for EE.
+constexpr int kEdgeTile = 2048;   // slots per tile, 8 per thread
+
+struct EdgeOffsets {
+    const uint32_t *eflag;
+    const unsigned short *ecnt;
+    const int4 *tvs;
+    const int32_t *deg;
+    int64_t n_slots;
+    int64_t *partials;   // 3 per tile
+    int64_t *et_off, *ef_off, *ee_off;
+    int64_t E;
+};
+
+__device__ __forceinline__ void slot_counts(const EdgeOffsets &p, long long s, int &et, int &ef,
+                                            int &ee)
+{
+    const unsigned short c = p.ecnt[s];
+    et = c & 0xff;
+    ef = c >> 8;
+    if (p.ee_off) {
+        const long long cell = s / 6;
+        const int j = (int)(s - 6 * cell);
+        const int4 w = __ldg(p.tvs + cell);
+        const int ia = j < 3 ? 0 : (j < 5 ? 1 : 2);
+        const int ib = j < 3 ? j + 1 : (j == 3 ? 2 : 3);
+        ee = __ldg(p.deg + get4(w, ia)) + __ldg(p.deg + get4(w, ib)) - 2;
+    } else {
+        ee = 0;
+    }
+}
+
+__device__ __forceinline__ void block_scan3(long long x[3], long long excl[3], long long tot[3])
+{
+    __shared__ long long sm[3][kThreads / 32 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        long long incl = x[q];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) sm[q][warp] = incl;
+        excl[q] = incl - x[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const long long w = lane < kThreads / 32 ? sm[q][lane] : 0;
+            long long wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            if (lane < kThreads / 32) sm[q][lane] = wi - w;
+            if (lane == kThreads / 32 - 1) sm[q][kThreads / 32] = wi;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        excl[q] += sm[q][warp];
+        tot[q] = sm[q][kThreads / 32];
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t slot_bits8(const EdgeOffsets &p, long long s0)
+{
+    // 8 consecutive slots starting at a multiple of 8 lie in one 32-bit word
+    return s0 < p.n_slots ? (p.eflag[s0 >> 5] >> (s0 & 31)) & 0xffu : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) k_edge_offsets_reduce(EdgeOffsets p)
+{
+    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
+    long long x[3] = {0, 0, 0};
+    const uint32_t bits = slot_bits8(p, s0);
+    for (int i = 0; i < 8; i++) {
+        if (!((bits >> i) & 1u) || s0 + i >= p.n_slots) continue;
+        int et, ef, ee;
+        slot_counts(p, s0 + i, et, ef, ee);
+        x[0] += et;
+        x[1] += ef;
+        x[2] += ee;
+    }
+    long long excl[3], tot[3];
+    block_scan3(x, excl, tot);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++) p.partials[3 * blockIdx.x + q] = tot[q];
+}
+
+__global__ void __launch_bounds__(1024) k_edge_offsets_partials(EdgeOffsets p, int64_t n_tiles)
+{
+    // one block: exclusive scan of the per-tile triples, 1024 tiles at a time
+    __shared__ long long sm[3][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long carry[3] = {0, 0, 0};
+    for (long long b = 0; b < n_tiles; b += 1024) {
+        const long long i = b + threadIdx.x;
+        for (int q = 0; q < 3; q++) {
+            const long long x = i < n_tiles ? p.partials[3 * i + q] : 0;
+            long long incl = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) sm[q][warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                const long long w = sm[q][lane];
+                long long wi = w;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long y = __shfl_up_sync(0xffffffffu, wi, o);
+                    if (lane >= o) wi += y;
+                }
+                sm[q][lane] = wi - w;
+                if (lane == 31) sm[q][32] = wi;
+            }
+            __syncthreads();
+            if (i < n_tiles) p.partials[3 * i + q] = carry[q] + sm[q][warp] + incl - x;
+            carry[q] += sm[q][32];
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (p.et_off) p.et_off[p.E] = carry[0];
+        if (p.ef_off) p.ef_off[p.E] = carry[1];
+        if (p.ee_off) p.ee_off[p.E] = carry[2];
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_edge_offsets_down(EdgeOffsets p, const uint2 *erank)
+{
+    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
+    long long x[3] = {0, 0, 0};
+    const uint32_t bits = slot_bits8(p, s0);
+    int et[8], ef[8], ee[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        et[i] = ef[i] = ee[i] = 0;
+        if (!((bits >> i) & 1u) || s0 + i >= p.n_slots) continue;
+        slot_counts(p, s0 + i, et[i], ef[i], ee[i]);
+        x[0] += et[i];
+        x[1] += ef[i];
+        x[2] += ee[i];
+    }
+    long long excl[3], tot[3];
+    block_scan3(x, excl, tot);
+    long long run[3];
+    for (int q = 0; q < 3; q++) run[q] = p.partials[3 * blockIdx.x + q] + excl[q];
+    if (!bits) return;
+    int id = rank_of(erank, s0);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        if (!((bits >> i) & 1u)) continue;
+        if (p.et_off) p.et_off[id] = run[0];
+        if (p.ef_off) p.ef_off[id] = run[1];
+        if (p.ee_off) p.ee_off[id] = run[2];
+        run[0] += et[i];
+        run[1] += ef[i];
+        run[2] += ee[i];
+        id++;
+    }
+}
+
+// win[w] = first vertex whose row starts at or after entry kWin * w, for
+// w in [0, n_win], with win[n_win] = V.  Vertex v owns the windows w with
+// off[v-1] < kWin * w <= off[v].
+__global__ void __launch_bounds__(256)
+k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int *__restrict__ win)
+{
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v > V) return;
+    const long long lo = v == 0 ? -1 : off[v - 1];
+    const long long hi = v == V ? (long long)kWin * n_win : off[v];
+    long long w = lo < 0 ? 0 : lo / kWin + 1;
+    const long long w_hi = hi / kWin;
+    for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
+}
+
+inline unsigned n_windows(int64_t nvt) { return (unsigned)(nvt / kWin + 1); }
+
+}  // namespace
+
+int64_t window_count(int64_t n_entries) { return n_entries / kWin + 1; }
+
+void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int32_t *win,
+                          cudaStream_t s)
+{
+    Launch L("k_window_starts", s);
+    k_window_starts<<<(unsigned)((V + 1 + 255) / 256), 256, 0, s>>>(off, V, window_count(n_entries),
+                                                                    win);
+}
+
+size_t edge_offsets_scratch_bytes(int64_t n_slots)
+{
+    return (size_t)(3 * (n_slots / kEdgeTile + 2)) * sizeof(int64_t);
+}
+
+void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
+                         const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
+                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, void *scratch,
+                         cudaStream_t s)
+{
+    EdgeOffsets p{eflag, reinterpret_cast<const unsigned short *>(ecnt), tvs, deg, n_slots,
+                  (int64_t *)scratch, et_off, ef_off, ee_off, E};
+    const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
+    if (tiles > 0) {
+        Launch L("k_edge_offsets_reduce", s);
+        k_edge_offsets_reduce<<<(unsigned)tiles, kThreads, 0, s>>>(p);
+    }
+    {
+        Launch L("k_edge_offsets_partials", s);
+        k_edge_offsets_partials<<<1, 1024, 0, s>>>(p, tiles);
+    }
+    if (tiles > 0) {
+        Launch L("k_edge_offsets_down", s);
+        k_edge_offsets_down<<<(unsigned)tiles, kThreads, 0, s>>>(p, erank);
+    }
+}
+
+void launch_star_a(const StarA &a, cudaStream_t s)
+{
+    if (a.V == 0) return;
+    Launch L("k_star_a", s);
+    k_star_a<<<n_windows(a.nvt), kThreads, 0, s>>>(a);
+}
+
+void launch_star_b(const StarB &b, cudaStream_t s)
+{
+    if (b.V == 0) return;
+    Launch L("k_star_b", s);
+    k_star_b<<<n_windows(b.nvt), kThreads, 0, s>>>(b);
+}
+
+void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
+                    int64_t nvt, cudaStream_t s)
+{
+    if (V == 0) return;
+    Launch L("k_vt_sort", s);
+    k_vt_sort<<<n_windows(nvt), kThreads, 0, s>>>(vt_off, win, vt);
+}
+
+}  // namespace tg
