@@ -157,6 +157,28 @@ int64_t tg_mesh_device_bytes(const tg_mesh *mesh);
 /* Number of kernel launches this library has issued in this process. */
 int64_t tg_kernel_launch_count(void);
 
+/* Critical points for callers that cannot allocate device memory: code
+ * running while a stream is being captured (no cudaMalloc there), a host
+ * application that gives this library a fixed memory budget up front, a
+ * real-time loop that forbids allocator calls after start-up.  No
+ * counterpart in the reference.  Inputs and output are device memory the
+ * caller owns: VV as CSR (vv_off [n_verts + 1], vv [n_vv_entries], rows
+ * sorted, as tg_get_relation returns it), the field (TG_FIELD_F32/F64,
+ * n_verts values) and classes_out (uint32 [n_verts x 3], the layout of
+ * tg_critical_points).  The link adjacency goes to a fixed device array of
+ * TG_NOALLOC_MAX_VV_ENTRIES 64-bit masks (64 MiB, plus a 128 KiB window table)
+ * that every GPU loading the library holds until the process exits; larger VV
+ * is rejected with
+ * TG_ERR_UNSUPPORTED.  The first call on a device looks up that array's
+ * device address, so make it before any stream capture begins.  Calls share
+ * the array: calls that overlap on the GPU race, so serialise them.  The
+ * call waits for its stream to read the kernels' status word.  Nothing is
+ * allocated (no cudaMalloc, cudaFree or allocating library routine). */
+#define TG_NOALLOC_MAX_VV_ENTRIES (1 << 23)
+tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int32_t *vv, int64_t n_verts,
+                                     int64_t n_vv_entries, const void *field, int field_type,
+                                     uint32_t *classes_out, void *stream);
+
 /* Time every launch of one kernel (by name, e.g. "k_star_b") with CUDA
  * events recorded on the stream it is launched on; NULL or "" turns timing
  * off.  For measurement tools; the reference's analogue is its Timer class
