@@ -133,6 +133,22 @@ tg_status tg_get_relation(const tg_mesh *mesh, int relation, const int64_t **off
 tg_status tg_copy_relation(const tg_mesh *mesh, int relation, int64_t *offsets_host,
                            int32_t *entries_host, void *stream);
 
+/* A relation's entries widened to int64 (the reference's vtkIdType) and its
+ * int64 offsets (CSR only; may be NULL), into caller memory on the device
+ * (out_on_device = 1, stream-ordered) or the host (0, synchronous).  Serves
+ * callers of the make_X_GPU_return functions, which returned vtkIdType device
+ * arrays (include/cuda_extraction.h:27-138). */
+tg_status tg_export_relation_i64(const tg_mesh *mesh, int relation, int64_t *entries_out,
+                                 int64_t *offsets_out, int out_on_device, void *stream);
+
+/* A CSR relation in the reference's padded device_VV layout
+ * (src/cuda_extraction.cu:1180-1274, read by the critPoints kernel): row r at
+ * padded_out[r * width], int64 entries, unused slots -1, and row lengths in
+ * counts_out (may be NULL).  Device memory, stream-ordered.  Rows longer than
+ * width are truncated: size width from the mesh (e.g. the largest VV row). */
+tg_status tg_export_rows_padded(const tg_mesh *mesh, int relation, int32_t width,
+                                int64_t *padded_out, uint32_t *counts_out, void *stream);
+
 /* Device pointer of the canonical (row-sorted) TV, int32 [n_cells x 4]. */
 tg_status tg_get_tv(const tg_mesh *mesh, const int32_t **tv_sorted);
 

@@ -63,6 +63,8 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_get_relation": (C.c_int, [vp, C.c_int, P(vp), P(vp), P(i64), P(i64), P(i32)]),
         "tg_copy_relation": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "tg_get_tv": (C.c_int, [vp, P(vp)]),
+        "tg_export_relation_i64": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp]),
+        "tg_export_rows_padded": (C.c_int, [vp, C.c_int, i32, vp, vp, vp]),
         "tg_critical_points": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]),
         "tg_mesh_device_bytes": (i64, [vp]),
         "tg_kernel_launch_count": (i64, []),

@@ -392,13 +392,6 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (et_off) tmp.p[tmp.n++] = et_off;
         if (ef_off) tmp.p[tmp.n++] = ef_off;
         if (ee_off) tmp.p[tmp.n++] = ee_off;
-        if (et_off || ef_off || ee_off) {
-            char *scratch2;
-            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T) + 256));
-            launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
-                                scratch2, s);
-        }
-
         // ---- pass B: ids, VV, fixed-width relations, ET and EF rows ----
         const bool need_ev = mask & (TG_EV | TG_EE);
         const bool need_te = mask & (TG_TE | TG_FE);
@@ -417,6 +410,14 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
         if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
         if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
+        // id-ordered passes over the occurrence slots
+        if (et_off || ef_off || ee_off || ev) {
+            char *scratch2;
+            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T) + 256));
+            launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
+                                ev, scratch2, s);
+        }
+        if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, nwf, fv, ft, ff_off, s);
         // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
         // only when EE is wanted); TT and FF from the boundary-face count
         int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
@@ -440,7 +441,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.vt_off = vt_off; b.win = m->vt_win; b.vt = vt; b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.vv = vv; b.eidv = eidv; b.eid_sorted = eid_sorted;
-        b.ev = ev; b.te = te; b.tf = tf; b.fv = fv; b.ft = ft; b.ff_off = ff_off;
+        b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
         launch_star_b(b, s);
         tmp.keep(vv);
@@ -576,8 +577,8 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     CK(cudaMemsetAsync(deg_t, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
     TRY(dalloc(&vt, 4 * T, s));
     launch_vt_fill(m->tvs, T, vt_off, deg_t, vt, s);
-    TRY(dalloc(&m->vt_win, window_count(4 * T) + 1, s));
-    launch_window_starts(vt_off, V, 4 * T, m->vt_win, s);
+    TRY(dalloc(&m->vt_win, window_count(4 * T, star_window()) + 1, s));
+    launch_window_starts(vt_off, V, 4 * T, star_window(), m->vt_win, s);
     launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, s);
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
@@ -669,6 +670,43 @@ tg_status tg_copy_relation(const tg_mesh *m, int r, int64_t *off_host, int32_t *
     return TG_OK;
 }
 
+tg_status tg_export_relation_i64(const tg_mesh *m, int r, int64_t *entries_out,
+                                 int64_t *offsets_out, int out_on_device, void *stream)
+{
+    if (!m || r < 1 || r > 13) return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh or relation index");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (entries_out && x.entries) {
+        int64_t *dst = entries_out;
+        Temps tmp(s);
+        if (!out_on_device) TRY(tmp.alloc(&dst, x.entries));
+        launch_widen(x.ent, dst, x.entries, s);
+        if (!out_on_device)
+            CK(cudaMemcpyAsync(entries_out, dst, (size_t)x.entries * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaGetLastError());
+    }
+    if (offsets_out && x.off)
+        CK(cudaMemcpyAsync(offsets_out, x.off, (size_t)(x.rows + 1) * 8,
+                           out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (!out_on_device) CK(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+
+tg_status tg_export_rows_padded(const tg_mesh *m, int r, int32_t width, int64_t *padded_out,
+                                uint32_t *counts_out, void *stream)
+{
+    if (!m || r < 1 || r > 13 || width < 0 || !padded_out)
+        return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh, relation index, width or output");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    if (!x.off) return fail(TG_ERR_INVALID_ARGUMENT, "relation %s is fixed width", kName[r]);
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_pad_rows(x.off, x.ent, x.rows, width, padded_out, counts_out, s);
+    CK(cudaGetLastError());
+    return TG_OK;
+}
+
 tg_status tg_get_tv(const tg_mesh *m, const int32_t **tv)
 {
     if (!m || !tv) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -691,8 +729,8 @@ tg_status tg_critical_points(tg_mesh *m, const void *field, int field_type, int 
         TRY(reset_status(m, s));
         TRY(dalloc(&m->cadj, vv.entries, s));
         int32_t *vv_win;
-        TRY(dalloc(&vv_win, window_count(vv.entries) + 1, s));
-        launch_window_starts(vv.off, V, vv.entries, vv_win, s);
+        TRY(dalloc(&vv_win, window_count(vv.entries, crit_window()) + 1, s));
+        launch_window_starts(vv.off, V, vv.entries, crit_window(), vv_win, s);
         // VV rows longer than the adjacency masks were already rejected by
         // tg_extract (star pass A flags them), so no status read-back here
         launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st, s);

@@ -155,12 +155,14 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 
 }  // namespace
 
+int crit_window() { return kAdjWin; }
+
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
                      int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
-    k_crit_adj<<<(unsigned)window_count(n_vv), kAdjWin, 0, s>>>(
+    k_crit_adj<<<(unsigned)window_count(n_vv, kAdjWin), kAdjWin, 0, s>>>(
         vv_off, vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
 }
 

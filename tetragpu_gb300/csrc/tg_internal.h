@@ -59,16 +59,20 @@ struct Sizes {
 };
 
 void launch_reset_status(DevStatus *st, cudaStream_t s);
+void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s);
+void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
+                     int64_t *out, uint32_t *counts, cudaStream_t s);
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
                   DevStatus *st, cudaStream_t s);
 void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, int32_t *cursor,
                     int32_t *vt, cudaStream_t s);
 void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStream_t s);
-// Windows of 256 entries over a CSR: win[w] = first row starting at or after
-// entry 256 w (w = 0 .. window_count), win[window_count] = rows.
-int64_t window_count(int64_t n_entries);
-void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int32_t *win,
-                          cudaStream_t s);
+// Windows of win_size entries over a CSR: win[w] = first row starting at or
+// after entry win_size * w (w = 0 .. window_count), win[window_count] = rows.
+int64_t window_count(int64_t n_entries, int win_size);
+void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int win_size,
+                          int32_t *win, cudaStream_t s);
+int star_window();  // the window size of the star kernels over VT
 // sort every VT row (tg_star.cu): window-staged, coalesced
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
                     int64_t nvt, cudaStream_t s);
@@ -91,10 +95,15 @@ void launch_star_a(const StarA &a, cudaStream_t s);
 
 // ET / EF / EE offsets in edge-id order from one scan over the 6T edge slots
 size_t edge_offsets_scratch_bytes(int64_t n_slots);
+// (also writes EV when ev is given)
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
-                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, void *scratch,
-                         cudaStream_t s);
+                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
+                         void *scratch, cudaStream_t s);
+// FV, FT[f][0] and FF offsets in face-id order (nw = words of the face bitmap)
+void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
+                       const int4 *tvs, int64_t nw, int32_t *fv, int32_t *ft, int64_t *ff_off,
+                       cudaStream_t s);
 
 struct StarB {
     const int64_t *vt_off;
@@ -110,12 +119,9 @@ struct StarB {
     int32_t *vv;               // [2E] VV rows
     int32_t *eidv;             // [2E] edge id of every VV entry
     int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null
-    int32_t *ev;               // [2E] or null
     int32_t *te;               // [6T] or null
     int32_t *tf;               // [4T] or null
-    int32_t *fv;               // [3F] or null
-    int32_t *ft;               // [2F] or null
-    int64_t *ff_off;           // [F+1] or null
+    int32_t *ft;               // [2F] or null: writes FT[f][1]
     const int64_t *et_off;
     int32_t *et;               // or null
     const int64_t *ef_off;
@@ -139,7 +145,8 @@ void launch_tt_vertex_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, co
                            const int64_t *tt_off, int32_t *tt, cudaStream_t s);
 
 // critical points (tg_crit.cu)
-// vv_win: window table of VV (launch_window_starts over vv_off)
+// vv_win: window table of VV (launch_window_starts over vv_off, crit_window())
+int crit_window();
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
                      int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s);
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,

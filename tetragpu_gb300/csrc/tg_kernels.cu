@@ -21,6 +21,7 @@
 //   k_star_a/b/c   the per-vertex star passes (tg_star.cu)
 //   k_cell_fe_tt   FE (from TE of a face's first cell) and face-sharing TT
 //   k_ff_fill      FF;  k_ee_fill  EE;  k_tt_vertex_*  vertex-sharing TT
+#include <algorithm>
 #include <climits>
 
 #include "tg_internal.h"
@@ -245,66 +246,68 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
     for (int i = 0; i < n; i++) row[i] = r[i];
 }
 
-// EE: a block takes 64 consecutive edges; thread (edge, side) stages the
-// sorted incident-edge row of one endpoint in shared memory, then places each
-// element at its rank in the merged row: an element x of one row has k
-// smaller elements in its own row and lower_bound(x) in the other; both rows
-// hold e itself once (and share nothing else), so its slot in e's EE row is
-// k + lower_bound - 2 * (e < x).
-constexpr int kEeEdges = 64;
+// EE: one warp per edge e = (a, b).  The sorted incident-edge rows of a and
+// b (at most kMaxDeg = 64 each) sit in the lanes, two per lane.  An element x
+// of one row with k smaller elements in its own row and lower_bound(x) in
+// the other lands at k + lower_bound - 2 * (e < x) in e's EE row: both rows
+// hold e itself once and share nothing else.  lower_bound is a binary
+// search whose probes read the other row through shuffles.
+constexpr int kEeWarps = 8;
 
-__device__ __forceinline__ int lower_bound_s(const int *a, int n, int key)
+__device__ __forceinline__ int row_at(int lo_half, int hi_half, int i)
 {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int m = (lo + hi) >> 1;
-        if (a[m] < key) lo = m + 1; else hi = m;
+    // element i (0..63) of a row held as lanes 0..31 (lo) and 32..63 (hi)
+    const int a = __shfl_sync(0xffffffffu, lo_half, i & 31);
+    const int b = __shfl_sync(0xffffffffu, hi_half, i & 31);
+    return i < 32 ? a : b;
+}
+
+__device__ __forceinline__ int warp_lower_bound(int lo_half, int hi_half, int n, int key)
+{
+    // all lanes run the same number of steps; each searches for its own key
+    int lo = 0, len = n;
+    while (__any_sync(0xffffffffu, len > 0)) {
+        const int half = len >> 1;
+        const int mid = min(lo + half, 63);
+        const int v = row_at(lo_half, hi_half, mid);
+        if (len > 0) {
+            if (v < key) {
+                lo = lo + half + 1;
+                len = len - half - 1;
+            } else {
+                len = half;
+            }
+        }
     }
     return lo;
 }
 
-__global__ void __launch_bounds__(2 * kEeEdges)
+__global__ void __launch_bounds__(kEeWarps * 32)
 k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_off,
           const int *__restrict__ eid, const int64_t *__restrict__ ee_off, int *__restrict__ ee)
 {
-    __shared__ int rows[2 * kEeEdges][kMaxDeg];
-    __shared__ int len[2 * kEeEdges];
-    __shared__ long long start[2 * kEeEdges];
-    const int64_t e0 = (int64_t)blockIdx.x * kEeEdges;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // where the rows are: one thread per (edge, side), all in flight at once
-    {
-        const int r = threadIdx.x;
-        const int64_t e = e0 + (r >> 1);
-        int n = 0;
-        long long b = 0;
-        if (e < E) {
-            const int v = __ldg(ev + 2 * e + (r & 1));
-            b = __ldg(vv_off + v);
-            n = (int)(__ldg(vv_off + v + 1) - b);
-        }
-        start[r] = b;
-        len[r] = n;
-    }
-    __syncthreads();
-    // copy: each warp moves 32 rows, lanes along a row (coalesced)
-#pragma unroll 4
-    for (int r = warp * 32; r < warp * 32 + 32; r++) {
-        const int n = len[r];
-        const long long b = start[r];
-        for (int k = lane; k < n; k += 32) rows[r][k] = __ldg(eid + b + k);
-    }
-    __syncthreads();
-    const int r = threadIdx.x;
-    const int64_t e = e0 + (r >> 1);
-    if (e >= E) return;
-    const int *mine = rows[r], *other = rows[r ^ 1];
-    const int nm = len[r], no = len[r ^ 1];
-    int *out = ee + ee_off[e];
-    for (int k = 0; k < nm; k++) {
-        const int x = mine[k];
-        if (x == (int)e) continue;
-        out[k + lower_bound_s(other, no, x) - 2 * ((int)e < x)] = x;
+    const int lane = threadIdx.x & 31;
+    const int64_t e = (int64_t)blockIdx.x * kEeWarps + (threadIdx.x >> 5);
+    if (e >= E) return;  // warp-uniform
+    const int2 ab = __ldg(reinterpret_cast<const int2 *>(ev) + e);
+    const int64_t ra = __ldg(vv_off + ab.x), rb = __ldg(vv_off + ab.y);
+    const int na = (int)(__ldg(vv_off + ab.x + 1) - ra), nb = (int)(__ldg(vv_off + ab.y + 1) - rb);
+    const int big = 0x7fffffff;
+    const int a0 = lane < na ? __ldg(eid + ra + lane) : big;
+    const int a1 = lane + 32 < na ? __ldg(eid + ra + lane + 32) : big;
+    const int b0 = lane < nb ? __ldg(eid + rb + lane) : big;
+    const int b1 = lane + 32 < nb ? __ldg(eid + rb + lane + 32) : big;
+    int *out = ee + __ldg(ee_off + e);
+    const int ei = (int)e;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int k = lane + 32 * h;
+        const int xa = h ? a1 : a0, xb = h ? b1 : b0;
+        if (h == 1 && na <= 32 && nb <= 32) break;   // warp-uniform
+        const int pa = warp_lower_bound(b0, b1, nb, xa);
+        const int pb = warp_lower_bound(a0, a1, na, xb);
+        if (k < na && xa != ei) out[k + pa - 2 * (ei < xa)] = xa;
+        if (k < nb && xb != ei) out[k + pb - 2 * (ei < xb)] = xb;
     }
 }
 
@@ -345,6 +348,31 @@ k_tt_vertex(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__
     if (!FILL) cnt[c] = n;
 }
 
+// int32 -> int64 (the reference's vtkIdType) copy
+__global__ void __launch_bounds__(256)
+k_widen(const int *__restrict__ src, long long *__restrict__ dst, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// CSR rows -> the reference's padded device_VV layout: row v at v * width,
+// unused slots -1, plus the row lengths
+__global__ void __launch_bounds__(256)
+k_pad_rows(const int64_t *__restrict__ off, const int *__restrict__ ent, int64_t rows, int width,
+           long long *__restrict__ out, unsigned *__restrict__ counts)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * width) return;
+    const int64_t r = i / width;
+    const int k = (int)(i - r * width);
+    const int64_t b = off[r];
+    const int n = (int)(off[r + 1] - b);
+    out[i] = k < n ? (long long)ent[b + k] : -1ll;
+    if (k == 0 && counts) counts[r] = (unsigned)n;
+}
+
 __global__ void k_reset_status(DevStatus *st)
 {
     st->flags = 0;
@@ -364,6 +392,23 @@ inline unsigned blocks_for(int64_t n, int threads)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s)
+{
+    if (n == 0) return;
+    Launch L("k_widen", s);
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
+    k_widen<<<(unsigned)blocks, 256, 0, s>>>(src, reinterpret_cast<long long *>(dst), n);
+}
+
+void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
+                     int64_t *out, uint32_t *counts, cudaStream_t s)
+{
+    if (rows == 0 || width == 0) return;
+    Launch L("k_pad_rows", s);
+    k_pad_rows<<<blocks_for(rows * width, 256), 256, 0, s>>>(off, ent, rows, width,
+                                                            reinterpret_cast<long long *>(out), counts);
+}
+
 void launch_reset_status(DevStatus *st, cudaStream_t s)
 {
     Launch L("k_reset_status", s);
@@ -432,7 +477,7 @@ void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const i
     if (E == 0) return;
     {
         Launch L("k_ee_fill", s);
-        k_ee_fill<<<blocks_for(E, kEeEdges), 2 * kEeEdges, 0, s>>>(ev, E, vv_off, eid_sorted,
+        k_ee_fill<<<blocks_for(E, kEeWarps), kEeWarps * 32, 0, s>>>(ev, E, vv_off, eid_sorted,
                                                                    ee_off, ee);
     }
 }

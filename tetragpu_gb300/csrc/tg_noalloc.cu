@@ -24,6 +24,7 @@ namespace {
 // race on it; serialise them.
 static __device__ __align__(256) unsigned long long g_noalloc_adj[TG_NOALLOC_MAX_VV_ENTRIES];
 static __device__ __align__(256) int g_noalloc_win[TG_NOALLOC_MAX_VV_ENTRIES / 256 + 2];
+// (the window table of the adjacency kernel: 256-entry windows over VV)
 static __device__ __align__(256) tg::DevStatus g_noalloc_status;
 
 constexpr int kMaxDevices = 64;
@@ -99,7 +100,7 @@ extern "C" tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int
     // window table and every adjacency mask are rewritten before they are read
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(tg::DevStatus), s);
     if (e != cudaSuccess) return fail(TG_ERR_CUDA, "clearing the status word", e);
-    tg::launch_window_starts(vv_off, n_verts, n_vv_entries, (int32_t *)win, s);
+    tg::launch_window_starts(vv_off, n_verts, n_vv_entries, tg::crit_window(), (int32_t *)win, s);
     tg::launch_crit_adj(vv_off, vv, (const int32_t *)win, n_verts, n_vv_entries, (uint64_t *)adj,
                         (tg::DevStatus *)status, s);
     tg::launch_crit_classify(vv_off, vv, (const uint64_t *)adj, field, field_type, n_verts,

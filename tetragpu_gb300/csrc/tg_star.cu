@@ -25,17 +25,30 @@
 //             ET / EF row lengths at each owned edge's first-occurrence slot,
 //             and neighbour counts
 //   k_star_b  ids (ranks of first occurrences), sorted VV rows, incident edge
-//             ids (by neighbour and by id), EV, TE, TF, FV, FT, FF offsets,
-//             ET and EF rows
+//             ids (by neighbour and by id), TE, TF, FT's second cell, ET and
+//             EF rows
+//   k_edge_offsets_* / k_face_slots  the id-ordered passes over occurrence
+//             slots: ET / EF / EE offsets and EV; FV, FT's first cell, FF
+//             offsets
 #include "tg_internal.h"
 
 namespace tg {
 namespace {
 
-constexpr int kWin = 256;                 // VT entries per block window
+#ifndef TG_STAR_WIN
+#define TG_STAR_WIN 256
+#endif
+#ifndef TG_STAR_THREADS
+#define TG_STAR_THREADS 256
+#endif
+#ifndef TG_STAR_HASH_BITS
+#define TG_STAR_HASH_BITS 10
+#endif
+constexpr int kWin = TG_STAR_WIN;         // VT entries per block window
 constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in the window)
-constexpr int kThreads = 256;
-constexpr int kHash = 1024;               // (vertex, neighbour) slots per block
+constexpr int kThreads = TG_STAR_THREADS;
+constexpr int kHashBits = TG_STAR_HASH_BITS;
+constexpr int kHash = 1 << kHashBits;     // (vertex, neighbour) slots per block, >= 3 * kCap
 constexpr unsigned long long kEmpty = ~0ull;
 
 __device__ __forceinline__ int get4(const int4 &w, int i)
@@ -72,31 +85,34 @@ struct Stage {
     int meta[kCap];                     // row start | D << 10 | slot of v << 20
     unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
     unsigned long long hmask[kHash];    // star positions whose cell holds the neighbour
-    int hval[kHash];                    // pass B: edge id of (v, neighbour)
     short cslot[kCap][4];               // hash slot of each entry's 3 candidates (other vertices)
-    int cnt[kCap];                      // per row start: neighbours listed so far
-    int list[3 * kCap];                 // per row start rs: its neighbours' hash slots at 3*rs..
+    int cnt[kCap];                      // per row start: neighbours counted / listed so far
     int n, vlo, vhi, full;
     long long base;
 };
+
+// static shared memory is capped at 48 KiB per block
+static_assert(sizeof(Stage) <= 48 * 1024, "star stage exceeds the static shared-memory limit");
+
+// pass B also lists each vertex's neighbours (at 3 * row start, the most a
+// row of D cells can have is 3D) with their edge ids
+struct StageB {
+    Stage S;
+    int hval[kHash];                    // list index, then edge id, of (v, neighbour)
+    int list_u[3 * kCap];
+    int list_id[3 * kCap];
+    int work[3 * kCap];                 // first sightings (entry << 2 | candidate) ...
+    int n_work, n_owned;                // ... the owned ones (u > v) first, then the rest
+};
+static_assert(sizeof(StageB) <= 48 * 1024, "star stage B exceeds the static shared-memory limit");
 
 __device__ __forceinline__ int m_rs(int m) { return m & 1023; }
 __device__ __forceinline__ int m_D(int m) { return (m >> 10) & 1023; }
 __device__ __forceinline__ int m_sv(int m) { return (m >> 20) & 3; }
 
-__device__ __forceinline__ int64_t lower_bound_g(const int64_t *a, int64_t n, int64_t key)
-{
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        const int64_t m = (lo + hi) >> 1;
-        if (a[m] < key) lo = m + 1; else hi = m;
-    }
-    return lo;
-}
-
 __device__ __forceinline__ unsigned hslot(unsigned long long key)
 {
-    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - 10));
+    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - kHashBits));
 }
 
 __device__ __forceinline__ int h_insert(Stage &S, unsigned long long key, unsigned long long bits)
@@ -311,74 +327,121 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
 {
-    __shared__ Stage S;
+    __shared__ StageB SB;
+    Stage &S = SB.S;
     if (!stage_and_hash(S, b.vt_off, b.win, b.vt, b.tvs, b.st, nullptr)) return;
     const int n = S.n;
 
-    // 1. list every vertex's neighbours (the hash slot of each first sighting)
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int rs = m_rs(S.meta[e]), pos = e - rs;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const int h = S.cslot[e][k];
-            if (ctz64(S.hmask[h]) == pos) S.list[3 * rs + atomicAdd(&S.cnt[rs], 1)] = h;
-        }
+    // 1. list every vertex's neighbours (each at its first sighting), and
+    //    collect the first sightings as one work list, owned edges first
+    if (threadIdx.x == 0) {
+        SB.n_work = 0;
+        SB.n_owned = 0;
     }
     __syncthreads();
-
-    // 2. per first sighting: edge id, VV position; for owned edges EV, ET, EF
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
         const int4 w = S.tv[e];
-        const int c = S.cell[e];
-        const int deg = S.cnt[rs];
-        const long long vvo = b.vv_off[v];
-#pragma unroll 1
+#pragma unroll
         for (int k = 0; k < 3; k++) {
             const int h = S.cslot[e][k];
+            if (ctz64(S.hmask[h]) != pos) continue;
+            const int u = get4(w, k + (k >= sv));
+            const int li = atomicAdd(&S.cnt[rs], 1);
+            SB.list_u[3 * rs + li] = u;
+            SB.hval[h] = li;
+            if (u > v) atomicAdd(&SB.n_owned, 1);
+        }
+    }
+    __syncthreads();
+    {
+        // owned first sightings fill work[0, n_owned), the others follow
+        __shared__ int s_o, s_r;
+        if (threadIdx.x == 0) {
+            s_o = 0;
+            s_r = SB.n_owned;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int v = S.vid[e], m = S.meta[e];
+            const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+            const int4 w = S.tv[e];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (ctz64(S.hmask[S.cslot[e][k]]) != pos) continue;
+                const int u = get4(w, k + (k >= sv));
+                const int at = u > v ? atomicAdd(&s_o, 1) : atomicAdd(&s_r, 1);
+                SB.work[at] = (e << 2) | k;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) SB.n_work = s_r;
+        __syncthreads();
+    }
+
+    // 2a. every first sighting: edge id and VV position
+    const int n_work = SB.n_work, n_owned = SB.n_owned;
+    for (int i = threadIdx.x; i < n_work; i += blockDim.x) {
+        const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
+        const int v = S.vid[e], m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m);
+        const int t = k + (k >= sv);
+        const int u = get4(S.tv[e], t);
+        const int h = S.cslot[e][k];
+        const int deg = S.cnt[rs];
+        const int *lu = SB.list_u + 3 * rs;
+        int rank = 0;
+        for (int j = 0; j < deg; j++) rank += lu[j] < u;
+        const int id = rank_of(b.erank, 6LL * S.cell[e] + pair_slot(min(sv, t), max(sv, t)));
+        SB.list_id[3 * rs + SB.hval[h]] = id;
+        SB.hval[h] = id;
+        const long long vvo = b.vv_off[v];
+        b.vv[vvo + rank] = u;
+        b.eidv[vvo + rank] = id;
+    }
+    __syncthreads();
+
+    // 2b. the edges v owns: ET rows (cells of the star holding u, ascending)
+    //     and EF rows (faces (v,u,x) at their first cell, cells ascending and
+    //     two faces of one cell by column: ascending first occurrence, which
+    //     is ascending face id)
+    if (b.et || b.ef) {
+        for (int i = threadIdx.x; i < n_owned; i += blockDim.x) {
+            const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
+            const int rs = m_rs(S.meta[e]), sv = m_sv(S.meta[e]);
+            const int u = get4(S.tv[e], k + (k >= sv));
+            const int h = S.cslot[e][k];
             const unsigned long long mu = S.hmask[h];
-            if (ctz64(mu) != pos) continue;
-            const int t = k + (k >= sv);
-            const int u = get4(w, t);
-            int rank = 0;
-            for (int i = 0; i < deg; i++) rank += (int)(unsigned)S.hkey[S.list[3 * rs + i]] < u;
-            const int id = rank_of(b.erank, 6LL * c + pair_slot(min(sv, t), max(sv, t)));
-            S.hval[h] = id;
-            b.vv[vvo + rank] = u;
-            b.eidv[vvo + rank] = id;
-            if (u <= v) continue;
-            if (b.ev) reinterpret_cast<int2 *>(b.ev)[id] = make_int2(v, u);
+            const int id = SB.hval[h];
             if (b.et) {
                 long long p = b.et_off[id];
                 for (unsigned long long mm = mu; mm; mm &= mm - 1) b.et[p++] = S.cell[rs + ctz64(mm)];
             }
             if (b.ef) {
-                const long long p0 = b.ef_off[id];
-                int cnt = 0;
+                long long p = b.ef_off[id];
                 for (unsigned long long mm = mu; mm; mm &= mm - 1) {
                     const int j = ctz64(mm);
                     const int ej = rs + j;
                     const int4 wj = S.tv[ej];
                     const int sj = m_sv(S.meta[ej]);
-                    const int ku = cand_of(slot_of(wj, u), sj);
+                    const int su = slot_of(wj, u);
+                    const int ku = cand_of(su, sj);
+                    int col[2], nf = 0;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
                         if (kk == ku) continue;
                         if (ctz64(mu & S.hmask[S.cslot[ej][kk]]) != j) continue;
                         const int tx = kk + (kk >= sj);
-                        // the face (v,u,x) omits the slot of cell j that is
-                        // neither v, u nor x: 6 - sj - su - tx
-                        const int of = 6 - sj - slot_of(wj, u) - tx;
-                        const int fid = rank_of(b.frank, 4LL * S.cell[ej] + (3 - of));
-                        long long i = p0 + cnt - 1;
-                        while (i >= p0 && b.ef[i] > fid) {
-                            b.ef[i + 1] = b.ef[i];
-                            i--;
-                        }
-                        b.ef[i + 1] = fid;
-                        cnt++;
+                        col[nf++] = 3 - (6 - sj - su - tx);   // the omitted slot is the fourth
                     }
+                    if (nf == 2 && col[0] > col[1]) {
+                        const int t2 = col[0];
+                        col[0] = col[1];
+                        col[1] = t2;
+                    }
+                    const long long q0 = 4LL * S.cell[ej];
+                    for (int f = 0; f < nf; f++) b.ef[p++] = rank_of(b.frank, q0 + col[f]);
                 }
             }
         }
@@ -386,56 +449,85 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
     __syncthreads();
 
     // 3. incident edge ids by id (for EE), TE entries of the pairs v is the
-    //    low end of, and the faces v owns
+    //    low end of, and TF / the second cell of the faces v owns
+    if (b.eid_sorted) {
+        for (int i = threadIdx.x; i < n_work; i += blockDim.x) {
+            const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
+            const int rs = m_rs(S.meta[e]);
+            const int id = SB.hval[S.cslot[e][k]];
+            const int deg = S.cnt[rs];
+            const int *li = SB.list_id + 3 * rs;
+            int r = 0;
+            for (int j = 0; j < deg; j++) r += li[j] < id;
+            b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
+        }
+    }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
         const int4 w = S.tv[e];
         const int c = S.cell[e];
-        if (b.eid_sorted) {
-            const int deg = S.cnt[rs];
-            const long long vvo = b.vv_off[v];
-            for (int k = 0; k < 3; k++) {
-                const int h = S.cslot[e][k];
-                if (ctz64(S.hmask[h]) != pos) continue;
-                const int id = S.hval[h];
-                int r = 0;
-                for (int i = 0; i < deg; i++) r += S.hval[S.list[3 * rs + i]] < id;
-                b.eid_sorted[vvo + r] = id;
-            }
-        }
         if (b.te) {
             for (int t = sv + 1; t < 4; t++)
-                b.te[6LL * c + pair_slot(sv, t)] = S.hval[S.cslot[e][cand_of(t, sv)]];
+                b.te[6LL * c + pair_slot(sv, t)] = SB.hval[S.cslot[e][cand_of(t, sv)]];
         }
-        if (sv <= 1 && (b.tf || b.fv || b.ft || b.ff_off)) {
+        if (sv <= 1 && (b.tf || b.ft)) {
             const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
             for (int o = o_lo; o <= o_hi; o++) {
-                int x, y;
-                face_others(w, sv, o, x, y);
                 const int ko = cand_of(o, sv);
                 const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
                 const unsigned long long mf =
                     S.hmask[S.cslot[e][ka]] & S.hmask[S.cslot[e][kb]];
                 const int j1 = ctz64(mf);
-                const int of = (j1 == pos) ? o : omitted_slot(S.tv[rs + j1], v, x, y);
+                int of = o;
+                if (j1 != pos) {
+                    int x, y;
+                    face_others(w, sv, o, x, y);
+                    of = omitted_slot(S.tv[rs + j1], v, x, y);
+                }
                 const long long q = 4LL * S.cell[rs + j1] + (3 - of);
                 const int fid = rank_of(b.frank, q);
                 if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                if (j1 != pos) continue;
-                const unsigned long long m2 = mf & (mf - 1);
-                const int c2 = m2 ? S.cell[rs + ctz64(m2)] : -1;
-                if (b.fv) {
-                    b.fv[3LL * fid] = v;
-                    b.fv[3LL * fid + 1] = x;
-                    b.fv[3LL * fid + 2] = y;
+                if (j1 == pos && b.ft) {
+                    const unsigned long long m2 = mf & (mf - 1);
+                    b.ft[2LL * fid + 1] = m2 ? S.cell[rs + ctz64(m2)] : -1;
                 }
-                if (b.ft) reinterpret_cast<int2 *>(b.ft)[fid] = make_int2(c, c2);
-                // a face's FF row holds 3 entries per cell of the face, so its
-                // offset is 3 * (2 fid - boundary faces before it)
-                if (b.ff_off) b.ff_off[fid] = 3LL * (2LL * fid - rank_of(b.brank, q));
             }
         }
+    }
+}
+
+// FV, FT's first cell and FF offsets in face-id order: one thread per 32
+// face-occurrence slots; a set bit is a face's first occurrence q = 4c + col,
+// the face omits slot 3 - col of cell c, and its id is its rank.
+__global__ void __launch_bounds__(256)
+k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank,
+             const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t nw,
+             int *__restrict__ fv, int *__restrict__ ft, int64_t *__restrict__ ff_off)
+{
+    const int64_t wd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (wd >= nw) return;
+    uint32_t bits = __ldg(fflag + wd);
+    int fid = (int)__ldg(frank + wd).y;
+    while (bits) {
+        const int i = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const long long q = 32LL * wd + i;
+        const long long c = q >> 2;
+        const int omit = 3 - (int)(q & 3);
+        if (fv) {
+            const int4 w = __ldg(tvs + c);
+            int o[3], k = 0;
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (t != omit) o[k++] = get4(w, t);
+            fv[3LL * fid] = o[0];
+            fv[3LL * fid + 1] = o[1];
+            fv[3LL * fid + 2] = o[2];
+        }
+        if (ft) ft[2LL * fid] = (int)c;
+        if (ff_off) ff_off[fid] = 3LL * (2LL * fid - rank_of(brank, q));
+        fid++;
     }
 }
 
@@ -507,6 +599,7 @@ struct EdgeOffsets {
     int64_t n_slots;
     int64_t *partials;   // 3 per tile
     int64_t *et_off, *ef_off, *ee_off;
+    int32_t *ev;         // [2E] or null: the edge's two vertices, ascending
     int64_t E;
 };
 
@@ -656,6 +749,14 @@ __global__ void __launch_bounds__(kThreads) k_edge_offsets_down(EdgeOffsets p, c
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         if (!((bits >> i) & 1u)) continue;
+        if (p.ev) {
+            const long long s = s0 + i, cell = s / 6;
+            const int j = (int)(s - 6 * cell);
+            const int4 w = __ldg(p.tvs + cell);
+            const int ia = j < 3 ? 0 : (j < 5 ? 1 : 2);
+            const int ib = j < 3 ? j + 1 : (j == 3 ? 2 : 3);
+            reinterpret_cast<int2 *>(p.ev)[id] = make_int2(get4(w, ia), get4(w, ib));
+        }
         if (p.et_off) p.et_off[id] = run[0];
         if (p.ef_off) p.ef_off[id] = run[1];
         if (p.ee_off) p.ee_off[id] = run[2];
@@ -670,14 +771,15 @@ __global__ void __launch_bounds__(kThreads) k_edge_offsets_down(EdgeOffsets p, c
 // w in [0, n_win], with win[n_win] = V.  Vertex v owns the windows w with
 // off[v-1] < kWin * w <= off[v].
 __global__ void __launch_bounds__(256)
-k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int *__restrict__ win)
+k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int win_size,
+                int *__restrict__ win)
 {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v > V) return;
     const long long lo = v == 0 ? -1 : off[v - 1];
-    const long long hi = v == V ? (long long)kWin * n_win : off[v];
-    long long w = lo < 0 ? 0 : lo / kWin + 1;
-    const long long w_hi = hi / kWin;
+    const long long hi = v == V ? (long long)win_size * n_win : off[v];
+    long long w = lo < 0 ? 0 : lo / win_size + 1;
+    const long long w_hi = hi / win_size;
     for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
 }
 
@@ -685,14 +787,16 @@ inline unsigned n_windows(int64_t nvt) { return (unsigned)(nvt / kWin + 1); }
 
 }  // namespace
 
-int64_t window_count(int64_t n_entries) { return n_entries / kWin + 1; }
+int star_window() { return kWin; }
 
-void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int32_t *win,
-                          cudaStream_t s)
+int64_t window_count(int64_t n_entries, int win_size) { return n_entries / win_size + 1; }
+
+void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int win_size,
+                          int32_t *win, cudaStream_t s)
 {
     Launch L("k_window_starts", s);
-    k_window_starts<<<(unsigned)((V + 1 + 255) / 256), 256, 0, s>>>(off, V, window_count(n_entries),
-                                                                    win);
+    k_window_starts<<<(unsigned)((V + 1 + 255) / 256), 256, 0, s>>>(
+        off, V, window_count(n_entries, win_size), win_size, win);
 }
 
 size_t edge_offsets_scratch_bytes(int64_t n_slots)
@@ -702,11 +806,11 @@ size_t edge_offsets_scratch_bytes(int64_t n_slots)
 
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
-                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, void *scratch,
-                         cudaStream_t s)
+                         int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
+                         void *scratch, cudaStream_t s)
 {
     EdgeOffsets p{eflag, reinterpret_cast<const unsigned short *>(ecnt), tvs, deg, n_slots,
-                  (int64_t *)scratch, et_off, ef_off, ee_off, E};
+                  (int64_t *)scratch, et_off, ef_off, ee_off, ev, E};
     const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
     if (tiles > 0) {
         Launch L("k_edge_offsets_reduce", s);
@@ -727,6 +831,16 @@ void launch_star_a(const StarA &a, cudaStream_t s)
     if (a.V == 0) return;
     Launch L("k_star_a", s);
     k_star_a<<<n_windows(a.nvt), kThreads, 0, s>>>(a);
+}
+
+void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
+                       const int4 *tvs, int64_t nw, int32_t *fv, int32_t *ft, int64_t *ff_off,
+                       cudaStream_t s)
+{
+    if (nw == 0) return;
+    Launch L("k_face_slots", s);
+    k_face_slots<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(fflag, frank, brank, tvs, nw, fv, ft,
+                                                             ff_off);
 }
 
 void launch_star_b(const StarB &b, cudaStream_t s)
