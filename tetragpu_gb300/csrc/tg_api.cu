@@ -417,7 +417,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
                                 ev, scratch2, s);
         }
-        if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, nwf, fv, ft, ff_off, s);
+        if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, s);
         // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
         // only when EE is wanted); TT and FF from the boundary-face count
         int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,

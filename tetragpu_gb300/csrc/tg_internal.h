@@ -102,7 +102,7 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
                          void *scratch, cudaStream_t s);
 // FV, FT[f][0] and FF offsets in face-id order (nw = words of the face bitmap)
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
-                       const int4 *tvs, int64_t nw, int32_t *fv, int32_t *ft, int64_t *ff_off,
+                       const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,
                        cudaStream_t s);
 
 struct StarB {

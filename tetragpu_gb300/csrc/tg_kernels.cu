@@ -246,40 +246,68 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
     for (int i = 0; i < n; i++) row[i] = r[i];
 }
 
-// EE: one warp per edge e = (a, b).  The sorted incident-edge rows of a and
-// b (at most kMaxDeg = 64 each) sit in the lanes, two per lane.  An element x
-// of one row with k smaller elements in its own row and lower_bound(x) in
-// the other lands at k + lower_bound - 2 * (e < x) in e's EE row: both rows
-// hold e itself once and share nothing else.  lower_bound is a binary
-// search whose probes read the other row through shuffles.
+// EE: a warp takes 32 consecutive edges (each lane fetches one edge's
+// endpoints and offsets), then merges them one at a time.  For e = (a, b) the
+// sorted incident-edge rows of a and b (at most kMaxDeg = 64 each) form one
+// bitonic sequence over 32 * R positions (lane l holds positions l + 32 r):
+// a's row ascending in the first half, b's row descending in the second, both
+// padded with INT_MAX towards the middle.  One bitonic merge sorts it; e sits
+// twice at adjacent positions (it is in both rows, and the rows share nothing
+// else), so dropping both copies leaves e's EE row.  R = 1, 2 or 4 by the
+// longer row (16, 32, 64 entries).
 constexpr int kEeWarps = 8;
 
-__device__ __forceinline__ int row_at(int lo_half, int hi_half, int i)
+template <int R>
+__device__ __forceinline__ void ee_merge_one(const int *__restrict__ eid, int64_t ra, int na,
+                                             int64_t rb, int nb, int ei, int *__restrict__ out,
+                                             int lane)
 {
-    // element i (0..63) of a row held as lanes 0..31 (lo) and 32..63 (hi)
-    const int a = __shfl_sync(0xffffffffu, lo_half, i & 31);
-    const int b = __shfl_sync(0xffffffffu, hi_half, i & 31);
-    return i < 32 ? a : b;
-}
-
-__device__ __forceinline__ int warp_lower_bound(int lo_half, int hi_half, int n, int key)
-{
-    // all lanes run the same number of steps; each searches for its own key
-    int lo = 0, len = n;
-    while (__any_sync(0xffffffffu, len > 0)) {
-        const int half = len >> 1;
-        const int mid = min(lo + half, 63);
-        const int v = row_at(lo_half, hi_half, mid);
-        if (len > 0) {
-            if (v < key) {
-                lo = lo + half + 1;
-                len = len - half - 1;
-            } else {
-                len = half;
-            }
+    constexpr int N = 32 * R, H = N / 2;
+    int x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int p = lane + 32 * r;
+        if (p < H) {
+            x[r] = p < na ? __ldg(eid + ra + p) : INT_MAX;
+        } else {
+            const int j = N - 1 - p;
+            x[r] = j < nb ? __ldg(eid + rb + j) : INT_MAX;
         }
     }
-    return lo;
+    // strides >= 32: between registers
+#pragma unroll
+    for (int sr = R / 2; sr >= 1; sr >>= 1) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            if (r & sr) continue;
+            const int lo = min(x[r], x[r + sr]), hi = max(x[r], x[r + sr]);
+            x[r] = lo;
+            x[r + sr] = hi;
+        }
+    }
+    // strides 16 .. 1: between lanes
+#pragma unroll
+    for (int sl = 16; sl >= 1; sl >>= 1) {
+        const bool upper = lane & sl;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int y = __shfl_xor_sync(kFull, x[r], sl);
+            x[r] = upper ? max(x[r], y) : min(x[r], y);
+        }
+    }
+    // the first copy of e
+    int pe = N;
+#pragma unroll
+    for (int r = R - 1; r >= 0; r--) {
+        const unsigned m = __ballot_sync(kFull, x[r] == ei);
+        if (m) pe = 32 * r + __ffs(m) - 1;
+    }
+    const int n = na + nb;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int p = lane + 32 * r;
+        if (p < n && x[r] != ei) out[p - (p > pe ? 2 : 0)] = x[r];
+    }
 }
 
 __global__ void __launch_bounds__(kEeWarps * 32)
@@ -287,27 +315,31 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
           const int *__restrict__ eid, const int64_t *__restrict__ ee_off, int *__restrict__ ee)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t e = (int64_t)blockIdx.x * kEeWarps + (threadIdx.x >> 5);
-    if (e >= E) return;  // warp-uniform
-    const int2 ab = __ldg(reinterpret_cast<const int2 *>(ev) + e);
-    const int64_t ra = __ldg(vv_off + ab.x), rb = __ldg(vv_off + ab.y);
-    const int na = (int)(__ldg(vv_off + ab.x + 1) - ra), nb = (int)(__ldg(vv_off + ab.y + 1) - rb);
-    const int big = 0x7fffffff;
-    const int a0 = lane < na ? __ldg(eid + ra + lane) : big;
-    const int a1 = lane + 32 < na ? __ldg(eid + ra + lane + 32) : big;
-    const int b0 = lane < nb ? __ldg(eid + rb + lane) : big;
-    const int b1 = lane + 32 < nb ? __ldg(eid + rb + lane + 32) : big;
-    int *out = ee + __ldg(ee_off + e);
-    const int ei = (int)e;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int k = lane + 32 * h;
-        const int xa = h ? a1 : a0, xb = h ? b1 : b0;
-        if (h == 1 && na <= 32 && nb <= 32) break;   // warp-uniform
-        const int pa = warp_lower_bound(b0, b1, nb, xa);
-        const int pb = warp_lower_bound(a0, a1, na, xb);
-        if (k < na && xa != ei) out[k + pa - 2 * (ei < xa)] = xa;
-        if (k < nb && xb != ei) out[k + pb - 2 * (ei < xb)] = xb;
+    const int64_t e0 = ((int64_t)blockIdx.x * kEeWarps + (threadIdx.x >> 5)) * 32;
+    if (e0 >= E) return;  // warp-uniform
+    const int cnt = E - e0 < 32 ? (int)(E - e0) : 32;
+    int64_t my_ra = 0, my_rb = 0, my_out = 0;
+    int my_na = 0, my_nb = 0;
+    if (lane < cnt) {
+        const int2 ab = __ldg(reinterpret_cast<const int2 *>(ev) + e0 + lane);
+        my_ra = __ldg(vv_off + ab.x);
+        my_rb = __ldg(vv_off + ab.y);
+        my_na = (int)(__ldg(vv_off + ab.x + 1) - my_ra);
+        my_nb = (int)(__ldg(vv_off + ab.y + 1) - my_rb);
+        my_out = __ldg(ee_off + e0 + lane);
+    }
+    for (int j = 0; j < cnt; j++) {
+        const int64_t ra = __shfl_sync(kFull, my_ra, j), rb = __shfl_sync(kFull, my_rb, j);
+        const int na = __shfl_sync(kFull, my_na, j), nb = __shfl_sync(kFull, my_nb, j);
+        int *out = ee + __shfl_sync(kFull, my_out, j);
+        const int ei = (int)(e0 + j);
+        const int mx = max(na, nb);
+        if (mx <= 16)
+            ee_merge_one<1>(eid, ra, na, rb, nb, ei, out, lane);
+        else if (mx <= 32)
+            ee_merge_one<2>(eid, ra, na, rb, nb, ei, out, lane);
+        else
+            ee_merge_one<4>(eid, ra, na, rb, nb, ei, out, lane);
     }
 }
 
@@ -477,7 +509,7 @@ void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const i
     if (E == 0) return;
     {
         Launch L("k_ee_fill", s);
-        k_ee_fill<<<blocks_for(E, kEeWarps), kEeWarps * 32, 0, s>>>(ev, E, vv_off, eid_sorted,
+        k_ee_fill<<<blocks_for((E + 31) / 32, kEeWarps), kEeWarps * 32, 0, s>>>(ev, E, vv_off, eid_sorted,
                                                                    ee_off, ee);
     }
 }

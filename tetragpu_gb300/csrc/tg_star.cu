@@ -253,8 +253,12 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
 {
     __shared__ Stage S;
+    __shared__ int work[3 * kCap];      // first sightings of owned edges (entry << 2 | candidate)
+    __shared__ int n_work;
     if (!stage_and_hash(S, a.vt_off, a.win, a.vt, a.tvs, a.st, a.deg)) return;
     const int n = S.n;
+    if (threadIdx.x == 0) n_work = 0;
+    __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
@@ -265,31 +269,9 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
         for (int k = 0; k < 3; k++) cm[k] = S.hmask[S.cslot[e][k]];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const int t = k + (k >= sv);
-            const int u = get4(w, t);
-            const unsigned long long mu = cm[k];
-            if (ctz64(mu) != pos) continue;                     // not the first sighting
+            if (ctz64(cm[k]) != pos) continue;                  // not the first sighting
             atomicAdd(&S.cnt[rs], 1);
-            if (u <= v) continue;
-            // an edge v owns: flag its first occurrence, record its ET and EF
-            // row lengths at that occurrence slot.  A face (v,u,x) is counted
-            // in the first cell holding u and x.
-            const long long p = 6LL * c + pair_slot(sv, t);
-            set_bit(a.eflag, p);
-            int n_ef = 0;
-            for (unsigned long long mm = mu; mm; mm &= mm - 1) {
-                const int j = ctz64(mm);
-                const int ej = rs + j;
-                const int4 wj = S.tv[ej];
-                const int sj = m_sv(S.meta[ej]);
-                const int ku = cand_of(slot_of(wj, u), sj);
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    if (kk == ku) continue;
-                    n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
-                }
-            }
-            a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+            if (get4(w, k + (k >= sv)) > v) work[atomicAdd(&n_work, 1)] = (e << 2) | k;
         }
         if (sv <= 1) {
             // faces whose lowest vertex is v: omit slot 1, 2, 3 when v is in
@@ -312,6 +294,34 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
         }
     }
     __syncthreads();
+    // the edges v owns, one per thread: flag the first occurrence and record
+    // the ET and EF row lengths at that occurrence slot.  A face (v,u,x) is
+    // counted in the first cell holding u and x.
+    const int nw = n_work;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) {
+        const int e = work[i] >> 2, k = work[i] & 3;
+        const int m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m);
+        const int t = k + (k >= sv);
+        const int u = get4(S.tv[e], t);
+        const unsigned long long mu = S.hmask[S.cslot[e][k]];
+        const long long p = 6LL * S.cell[e] + pair_slot(sv, t);
+        set_bit(a.eflag, p);
+        int n_ef = 0;
+        for (unsigned long long mm = mu; mm; mm &= mm - 1) {
+            const int j = ctz64(mm);
+            const int ej = rs + j;
+            const int4 wj = S.tv[ej];
+            const int sj = m_sv(S.meta[ej]);
+            const int ku = cand_of(slot_of(wj, u), sj);
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++) {
+                if (kk == ku) continue;
+                n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
+            }
+        }
+        a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+    }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
         if (m_rs(m) != e) continue;
@@ -497,36 +507,44 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
     }
 }
 
-// FV, FT's first cell and FF offsets in face-id order: one thread per 32
-// face-occurrence slots; a set bit is a face's first occurrence q = 4c + col,
-// the face omits slot 3 - col of cell c, and its id is its rank.
+// The faces in id order, one thread per cell: the cell's first-occurrence
+// bits (4 per cell, 8 cells per flag word) with the rank of the first give
+// the ids of the faces first seen in it; writes FV, FT's first cell and the
+// FF offsets (3 * (2 * id - boundary faces before it)).
 __global__ void __launch_bounds__(256)
 k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank,
-             const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t nw,
+             const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t T,
              int *__restrict__ fv, int *__restrict__ ft, int64_t *__restrict__ ff_off)
 {
-    const int64_t wd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (wd >= nw) return;
-    uint32_t bits = __ldg(fflag + wd);
-    int fid = (int)__ldg(frank + wd).y;
-    while (bits) {
-        const int i = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const long long q = 32LL * wd + i;
-        const long long c = q >> 2;
-        const int omit = 3 - (int)(q & 3);
-        if (fv) {
-            const int4 w = __ldg(tvs + c);
-            int o[3], k = 0;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= T) return;
+    const int sh = (int)(c & 7) * 4;
+    const uint32_t word = __ldg(fflag + (c >> 3));
+    const uint32_t bits = (word >> sh) & 0xfu;
+    if (!bits) return;
+    const uint2 fr = __ldg(frank + (c >> 3));
+    int fid = (int)fr.y + __popc(word & ((1u << sh) - 1u));
+    const int4 w = __ldg(tvs + c);
+    uint2 br = make_uint2(0, 0);
+    if (ff_off) br = __ldg(brank + (c >> 3));
 #pragma unroll
-            for (int t = 0; t < 4; t++)
-                if (t != omit) o[k++] = get4(w, t);
-            fv[3LL * fid] = o[0];
-            fv[3LL * fid + 1] = o[1];
-            fv[3LL * fid + 2] = o[2];
+    for (int col = 0; col < 4; col++) {
+        if (!((bits >> col) & 1u)) continue;
+        if (fv) {
+            // the face omits slot 3 - col
+            const int o0 = col == 3 ? w.y : w.x;
+            const int o1 = col >= 2 ? w.z : w.y;
+            const int o2 = col >= 1 ? w.w : w.z;
+            fv[3LL * fid] = o0;
+            fv[3LL * fid + 1] = o1;
+            fv[3LL * fid + 2] = o2;
         }
         if (ft) ft[2LL * fid] = (int)c;
-        if (ff_off) ff_off[fid] = 3LL * (2LL * fid - rank_of(brank, q));
+        if (ff_off) {
+            const int qb = sh + col;
+            const int nb = (int)br.y + __popc(br.x & ((1u << qb) - 1u));
+            ff_off[fid] = 3LL * (2LL * fid - nb);
+        }
         fid++;
     }
 }
@@ -834,13 +852,13 @@ void launch_star_a(const StarA &a, cudaStream_t s)
 }
 
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
-                       const int4 *tvs, int64_t nw, int32_t *fv, int32_t *ft, int64_t *ff_off,
+                       const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,
                        cudaStream_t s)
 {
-    if (nw == 0) return;
+    if (T == 0) return;
     Launch L("k_face_slots", s);
-    k_face_slots<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(fflag, frank, brank, tvs, nw, fv, ft,
-                                                             ff_off);
+    k_face_slots<<<(unsigned)((T + 255) / 256), 256, 0, s>>>(fflag, frank, brank, tvs, T, fv, ft,
+                                                            ff_off);
 }
 
 void launch_star_b(const StarB &b, cudaStream_t s)
