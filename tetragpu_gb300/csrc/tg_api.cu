@@ -169,7 +169,7 @@ const char *kName[14] = {"validate", "TE", "EV", "ET", "TF", "FV", "FE",
 // Scoped list of stream-ordered temporaries, freed when the stage ends.
 struct Temps {
     cudaStream_t s;
-    void *p[32];
+    void *p[64];
     int n = 0;
     explicit Temps(cudaStream_t st) : s(st) {}
     ~Temps()
@@ -181,6 +181,7 @@ struct Temps {
     tg_status alloc(T **out, int64_t count, bool zero = false)
     {
         size_t b = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+        if (n >= 64) return fail(TG_ERR_UNSUPPORTED, "too many temporaries in one stage");
         void *q = nullptr;
         cudaError_t e = cudaMallocAsync(&q, b, s);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (temporary)", __LINE__);
@@ -192,6 +193,8 @@ struct Temps {
         *out = (T *)q;
         return TG_OK;
     }
+    // free q with the others if the stage fails (list sized for every path)
+    void track(void *q) { p[n++] = q; }
     // hand a temporary over to the caller (it is not freed here)
     void keep(void *q)
     {
@@ -350,13 +353,15 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (need_ecnt) TRY(tmp.alloc(&ecnt, 6 * T, true));
         TRY(tmp.alloc(&deg, V));
         TRY(dalloc(&vv_off, V + 1, s));
-        tmp.p[tmp.n++] = vv_off;  // owned by the VV relation once it is ready
+        tmp.track(vv_off);  // owned by the VV relation once it is ready
         char *scratch;
         const int64_t maxn = std::max(V, std::max(nwe, nwf));
         TRY(tmp.alloc(&scratch, 5 * (int64_t)(scan_scratch_bytes(maxn) + 256)));
         int64_t *deg_sq;  // prefix of deg^2: its total sizes EE (sum deg^2 - 2E)
         TRY(tmp.alloc(&deg_sq, V + 1));
-        StarA a{vt_off, m->vt_win, vt, m->tvs, V, NVT, deg, ecnt, eflag, fflag, fbnd, m->st};
+        uint64_t *emask;  // pass A's candidate masks, pass B's input
+        TRY(tmp.alloc(&emask, 3 * NVT));
+        StarA a{vt_off, m->vt_win, vt, m->tvs, V, NVT, deg, ecnt, eflag, fflag, fbnd, m->st, emask};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));
@@ -389,20 +394,19 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_ET) TRY(dalloc(&et_off, E + 1, s));
         if (mask & TG_EF) TRY(dalloc(&ef_off, E + 1, s));
         if (mask & TG_EE) TRY(dalloc(&ee_off, E + 1, s));
-        if (et_off) tmp.p[tmp.n++] = et_off;
-        if (ef_off) tmp.p[tmp.n++] = ef_off;
-        if (ee_off) tmp.p[tmp.n++] = ee_off;
+        if (et_off) tmp.track(et_off);
+        if (ef_off) tmp.track(ef_off);
+        if (ee_off) tmp.track(ee_off);
         // ---- pass B: ids, VV, fixed-width relations, ET and EF rows ----
         const bool need_ev = mask & (TG_EV | TG_EE);
         const bool need_te = mask & (TG_TE | TG_FE);
         const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF)) || want_tt_face;
         const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
-        int32_t *vv, *eidv, *eid_sorted = nullptr;
+        int32_t *vv, *eid_sorted = nullptr;
         int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
         int64_t *ff_off = nullptr;
         TRY(dalloc(&vv, nvv, s));
-        tmp.p[tmp.n++] = vv;
-        TRY(tmp.alloc(&eidv, nvv));
+        tmp.track(vv);
         if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
         if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
         if (need_te) TRY(tmp.alloc(&te, 6 * T));
@@ -440,7 +444,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         StarB b{};
         b.vt_off = vt_off; b.win = m->vt_win; b.vt = vt; b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
-        b.vv = vv; b.eidv = eidv; b.eid_sorted = eid_sorted;
+        b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
         launch_star_b(b, s);

@@ -90,6 +90,7 @@ struct StarA {
     uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
     uint32_t *fbnd;            // bit per face occurrence: first and only (boundary face)
     DevStatus *st;
+    uint64_t *emask;           // [3][nvt] star positions holding each entry's candidates
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
 
@@ -116,8 +117,8 @@ struct StarB {
     const uint2 *erank;        // {bits, prefix} per 32 edge occurrences
     const uint2 *frank;        // same for face occurrences
     const uint2 *brank;        // same for boundary-face occurrences
+    const uint64_t *emask;     // [3][nvt] from pass A
     int32_t *vv;               // [2E] VV rows
-    int32_t *eidv;             // [2E] edge id of every VV entry
     int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null
     int32_t *te;               // [6T] or null
     int32_t *tf;               // [4T] or null

@@ -94,17 +94,27 @@ struct Stage {
 // static shared memory is capped at 48 KiB per block
 static_assert(sizeof(Stage) <= 48 * 1024, "star stage exceeds the static shared-memory limit");
 
-// pass B also lists each vertex's neighbours (at 3 * row start, the most a
-// row of D cells can have is 3D) with their edge ids
-struct StageB {
-    Stage S;
-    int hval[kHash];                    // list index, then edge id, of (v, neighbour)
+// Pass B stages the same window without a hash: pass A leaves every VT
+// entry's three candidate masks in global memory.  It also lists each
+// vertex's neighbours (at 3 * row start, the most a row of D cells can have
+// is 3D) with their edge ids.
+struct StageM {
+    int cell[kCap];
+    int4 tv[kCap];
+    int vid[kCap];
+    int meta[kCap];                     // row start | D << 10 | slot of v << 20
+    unsigned long long cm[kCap][3];     // star positions holding each candidate
+    int hv[kCap][3];                    // at first sightings: list index, then edge id
+    int cnt[kCap];
     int list_u[3 * kCap];
     int list_id[3 * kCap];
-    int work[3 * kCap];                 // first sightings (entry << 2 | candidate) ...
-    int n_work, n_owned;                // ... the owned ones (u > v) first, then the rest
+    int work[3 * kCap];                 // first sightings (entry << 2 | candidate): n_owned
+                                        // owned ones (u > v) from the front, n_work others
+                                        // from the back
+    int n, vlo, vhi, n_work, n_owned;
+    long long base;
 };
-static_assert(sizeof(StageB) <= 48 * 1024, "star stage B exceeds the static shared-memory limit");
+static_assert(sizeof(StageM) <= 48 * 1024, "star stage B exceeds the static shared-memory limit");
 
 __device__ __forceinline__ int m_rs(int m) { return m & 1023; }
 __device__ __forceinline__ int m_D(int m) { return (m >> 10) & 1023; }
@@ -266,7 +276,10 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
         const int c = S.cell[e];
         unsigned long long cm[3];
 #pragma unroll
-        for (int k = 0; k < 3; k++) cm[k] = S.hmask[S.cslot[e][k]];
+        for (int k = 0; k < 3; k++) {
+            cm[k] = S.hmask[S.cslot[e][k]];
+            a.emask[k * a.nvt + S.base + e] = cm[k];
+        }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (ctz64(cm[k]) != pos) continue;                  // not the first sighting
@@ -335,174 +348,229 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
 }
 
 // ---------------------------------------------------------------------------
+// Stage pass B's window: rows, cells, cell vertices and the candidate
+// masks pass A computed.  Pass A has already rejected every window this
+// cannot hold, so nothing here fails.
+__device__ void stage_masks(StageM &S, const StarB &b)
+{
+    if (threadIdx.x == 0) {
+        const int vlo = b.win[blockIdx.x], vhi = b.win[blockIdx.x + 1];
+        S.vlo = vlo;
+        S.vhi = vhi;
+        S.base = b.vt_off[vlo];
+        S.n = (int)(b.vt_off[vhi] - S.base);
+        S.n_work = 0;
+        S.n_owned = 0;
+    }
+    __syncthreads();
+    const int n = S.n;
+    const long long base = S.base;
+    for (int v = S.vlo + threadIdx.x; v < S.vhi; v += blockDim.x) {
+        const int rs = (int)(b.vt_off[v] - base);
+        const int D = (int)(b.vt_off[v + 1] - b.vt_off[v]);
+        for (int i = 0; i < D; i++) {
+            S.vid[rs + i] = v;
+            S.meta[rs + i] = rs | (D << 10);
+        }
+        if (D > 0) S.cnt[rs] = 0;
+    }
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = __ldg(b.vt + base + e);
+        S.cell[e] = c;
+        S.tv[e] = __ldg(b.tvs + c);
+#pragma unroll
+        for (int k = 0; k < 3; k++) S.cm[e][k] = __ldg(b.emask + k * b.nvt + base + e);
+    }
+    __syncthreads();
+}
+
+// hv entry of candidate u of entry e: the one at u's first sighting in e's row
+__device__ __forceinline__ int hv_of(const StageM &S, int e, int k, int rs, int u)
+{
+    const int f = rs + ctz64(S.cm[e][k]);
+    if (f == e) return S.hv[e][k];
+    return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
+}
+
 __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
 {
-    __shared__ StageB SB;
-    Stage &S = SB.S;
-    if (!stage_and_hash(S, b.vt_off, b.win, b.vt, b.tvs, b.st, nullptr)) return;
+    __shared__ StageM S;
+    stage_masks(S, b);
     const int n = S.n;
 
-    // 1. list every vertex's neighbours (each at its first sighting), and
-    //    collect the first sightings as one work list, owned edges first
-    if (threadIdx.x == 0) {
-        SB.n_work = 0;
-        SB.n_owned = 0;
-    }
-    __syncthreads();
+    // 1. list every vertex's neighbours (each at its first sighting); the
+    //    first sightings form one work list, owned edges (u > v) from the
+    //    front, the others from the back
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int v = S.vid[e], m = S.meta[e];
-        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        const int rs = m_rs(m), pos = e - rs;
         const int4 w = S.tv[e];
+        const int sv = slot_of(w, v);
+        S.meta[e] = m | (sv << 20);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const int h = S.cslot[e][k];
-            if (ctz64(S.hmask[h]) != pos) continue;
+            if (ctz64(S.cm[e][k]) != pos) continue;
             const int u = get4(w, k + (k >= sv));
             const int li = atomicAdd(&S.cnt[rs], 1);
-            SB.list_u[3 * rs + li] = u;
-            SB.hval[h] = li;
-            if (u > v) atomicAdd(&SB.n_owned, 1);
+            S.list_u[3 * rs + li] = u;
+            S.hv[e][k] = li;
+            if (u > v)
+                S.work[atomicAdd(&S.n_owned, 1)] = (e << 2) | k;
+            else
+                S.work[3 * kCap - 1 - atomicAdd(&S.n_work, 1)] = (e << 2) | k;
         }
     }
     __syncthreads();
-    {
-        // owned first sightings fill work[0, n_owned), the others follow
-        __shared__ int s_o, s_r;
-        if (threadIdx.x == 0) {
-            s_o = 0;
-            s_r = SB.n_owned;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < n; e += blockDim.x) {
-            const int v = S.vid[e], m = S.meta[e];
-            const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
-            const int4 w = S.tv[e];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                if (ctz64(S.hmask[S.cslot[e][k]]) != pos) continue;
-                const int u = get4(w, k + (k >= sv));
-                const int at = u > v ? atomicAdd(&s_o, 1) : atomicAdd(&s_r, 1);
-                SB.work[at] = (e << 2) | k;
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) SB.n_work = s_r;
-        __syncthreads();
-    }
+    const int n_owned = S.n_owned, n_first = n_owned + S.n_work;
+    auto first_item = [&](int i) {
+        return i < n_owned ? S.work[i] : S.work[3 * kCap - 1 - (i - n_owned)];
+    };
 
-    // 2a. every first sighting: edge id and VV position
-    const int n_work = SB.n_work, n_owned = SB.n_owned;
-    for (int i = threadIdx.x; i < n_work; i += blockDim.x) {
-        const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
+    // 2. every first sighting: edge id and VV position
+    for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
+        const int it = first_item(i);
+        const int e = it >> 2, k = it & 3;
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m);
         const int t = k + (k >= sv);
         const int u = get4(S.tv[e], t);
-        const int h = S.cslot[e][k];
         const int deg = S.cnt[rs];
-        const int *lu = SB.list_u + 3 * rs;
+        const int *lu = S.list_u + 3 * rs;
         int rank = 0;
         for (int j = 0; j < deg; j++) rank += lu[j] < u;
         const int id = rank_of(b.erank, 6LL * S.cell[e] + pair_slot(min(sv, t), max(sv, t)));
-        SB.list_id[3 * rs + SB.hval[h]] = id;
-        SB.hval[h] = id;
-        const long long vvo = b.vv_off[v];
-        b.vv[vvo + rank] = u;
-        b.eidv[vvo + rank] = id;
+        S.list_id[3 * rs + S.hv[e][k]] = id;
+        S.hv[e][k] = id;
+        if (b.vv) b.vv[b.vv_off[v] + rank] = u;
     }
     __syncthreads();
 
-    // 2b. the edges v owns: ET rows (cells of the star holding u, ascending)
-    //     and EF rows (faces (v,u,x) at their first cell, cells ascending and
-    //     two faces of one cell by column: ascending first occurrence, which
-    //     is ascending face id)
+    // 3a. the edges v owns, four lanes to an edge, the lanes of an edge
+    //     taking its cells four at a time in ascending order: ET rows (cells
+    //     of the star holding u, ascending) and EF rows (faces (v,u,x) at
+    //     their first cell, cells ascending, two faces of one cell by column:
+    //     ascending first occurrence, which is ascending face id); a scan
+    //     over the four lanes places each cell's faces
     if (b.et || b.ef) {
-        for (int i = threadIdx.x; i < n_owned; i += blockDim.x) {
-            const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
-            const int rs = m_rs(S.meta[e]), sv = m_sv(S.meta[e]);
-            const int u = get4(S.tv[e], k + (k >= sv));
-            const int h = S.cslot[e][k];
-            const unsigned long long mu = S.hmask[h];
-            const int id = SB.hval[h];
-            if (b.et) {
-                long long p = b.et_off[id];
-                for (unsigned long long mm = mu; mm; mm &= mm - 1) b.et[p++] = S.cell[rs + ctz64(mm)];
+        const int span = ((n_owned * 4 + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+        for (int t = threadIdx.x; t < span; t += blockDim.x) {   // block-uniform trip count
+            const int i = t >> 2, sub = t & 3;
+            const bool act = i < n_owned;
+            int rs = 0, u = 0, id = 0;
+            unsigned long long mu = 0;
+            if (act) {
+                const int e = S.work[i] >> 2, k = S.work[i] & 3;
+                const int m = S.meta[e];
+                rs = m_rs(m);
+                u = get4(S.tv[e], k + (k >= m_sv(m)));
+                mu = S.cm[e][k];
+                id = S.hv[e][k];
             }
-            if (b.ef) {
-                long long p = b.ef_off[id];
-                for (unsigned long long mm = mu; mm; mm &= mm - 1) {
-                    const int j = ctz64(mm);
+            const int rounds = (__popcll(mu) + 3) >> 2;
+            const int max_rounds = __reduce_max_sync(0xffffffffu, rounds);
+            long long et_p = act && b.et ? b.et_off[id] : 0;
+            long long ef_p = act && b.ef ? b.ef_off[id] : 0;
+            unsigned long long rest = mu;
+            for (int r = 0; r < max_rounds; r++) {
+                // this lane's cell: the sub-th lowest remaining bit
+                unsigned long long mine = rest;
+                for (int q = 0; q < sub; q++) mine &= mine - 1;
+                const int j = mine ? ctz64(mine) : -1;
+                int nf = 0, col0 = 0, col1 = 0;
+                long long q0 = 0;
+                if (j >= 0) {
                     const int ej = rs + j;
+                    if (b.et) b.et[et_p + sub] = S.cell[ej];
                     const int4 wj = S.tv[ej];
                     const int sj = m_sv(S.meta[ej]);
                     const int su = slot_of(wj, u);
                     const int ku = cand_of(su, sj);
-                    int col[2], nf = 0;
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
                         if (kk == ku) continue;
-                        if (ctz64(mu & S.hmask[S.cslot[ej][kk]]) != j) continue;
+                        if (ctz64(mu & S.cm[ej][kk]) != j) continue;
                         const int tx = kk + (kk >= sj);
-                        col[nf++] = 3 - (6 - sj - su - tx);   // the omitted slot is the fourth
+                        const int c = 3 - (6 - sj - su - tx);   // the omitted slot is the fourth
+                        if (nf == 0) col0 = c; else col1 = c;
+                        nf++;
                     }
-                    if (nf == 2 && col[0] > col[1]) {
-                        const int t2 = col[0];
-                        col[0] = col[1];
-                        col[1] = t2;
+                    if (nf == 2 && col0 > col1) {
+                        const int t2 = col0;
+                        col0 = col1;
+                        col1 = t2;
                     }
-                    const long long q0 = 4LL * S.cell[ej];
-                    for (int f = 0; f < nf; f++) b.ef[p++] = rank_of(b.frank, q0 + col[f]);
+                    q0 = 4LL * S.cell[ej];
                 }
+                int x = nf;
+                int y = __shfl_up_sync(0xffffffffu, x, 1, 4);
+                if (sub >= 1) x += y;
+                y = __shfl_up_sync(0xffffffffu, x, 2, 4);
+                if (sub >= 2) x += y;
+                const int tot = __shfl_sync(0xffffffffu, x, 3, 4);
+                if (b.ef && nf > 0) {
+                    const long long p = ef_p + (x - nf);
+                    b.ef[p] = rank_of(b.frank, q0 + col0);
+                    if (nf == 2) b.ef[p + 1] = rank_of(b.frank, q0 + col1);
+                }
+                et_p += 4;
+                ef_p += tot;
+                rest &= rest - 1;
+                rest &= rest - 1;
+                rest &= rest - 1;
+                rest &= rest - 1;
             }
         }
     }
-    __syncthreads();
 
-    // 3. incident edge ids by id (for EE), TE entries of the pairs v is the
-    //    low end of, and TF / the second cell of the faces v owns
-    if (b.eid_sorted) {
-        for (int i = threadIdx.x; i < n_work; i += blockDim.x) {
-            const int e = SB.work[i] >> 2, k = SB.work[i] & 3;
+    // 3b. one pass over two kinds of items:
+    //    [0, n)          an entry: TE of the pairs v is the low end of, TF /
+    //                    FT's second cell of the faces v owns
+    //    then n_first    a first sighting: its place among v's incident edge
+    //                    ids (for EE)
+    const int n_items = n + (b.eid_sorted ? n_first : 0);
+    for (int i = threadIdx.x; i < n_items; i += blockDim.x) {
+        if (i < n) {
+            const int e = i;
+            const int v = S.vid[e], m = S.meta[e];
+            const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+            const int4 w = S.tv[e];
+            const int c = S.cell[e];
+            if (b.te) {
+                for (int t = sv + 1; t < 4; t++)
+                    b.te[6LL * c + pair_slot(sv, t)] = hv_of(S, e, cand_of(t, sv), rs, get4(w, t));
+            }
+            if (sv <= 1 && (b.tf || b.ft)) {
+                const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
+                for (int o = o_lo; o <= o_hi; o++) {
+                    const int ko = cand_of(o, sv);
+                    const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
+                    const unsigned long long mf = S.cm[e][ka] & S.cm[e][kb];
+                    const int j1 = ctz64(mf);
+                    int of = o;
+                    if (j1 != pos) {
+                        int x, y;
+                        face_others(w, sv, o, x, y);
+                        of = omitted_slot(S.tv[rs + j1], v, x, y);
+                    }
+                    const long long q = 4LL * S.cell[rs + j1] + (3 - of);
+                    const int fid = rank_of(b.frank, q);
+                    if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
+                    if (j1 == pos && b.ft) {
+                        const unsigned long long m2 = mf & (mf - 1);
+                        b.ft[2LL * fid + 1] = m2 ? S.cell[rs + ctz64(m2)] : -1;
+                    }
+                }
+            }
+        } else {
+            const int it = first_item(i - n);
+            const int e = it >> 2, k = it & 3;
             const int rs = m_rs(S.meta[e]);
-            const int id = SB.hval[S.cslot[e][k]];
+            const int id = S.hv[e][k];
             const int deg = S.cnt[rs];
-            const int *li = SB.list_id + 3 * rs;
+            const int *li = S.list_id + 3 * rs;
             int r = 0;
             for (int j = 0; j < deg; j++) r += li[j] < id;
             b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
-        }
-    }
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int v = S.vid[e], m = S.meta[e];
-        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
-        const int4 w = S.tv[e];
-        const int c = S.cell[e];
-        if (b.te) {
-            for (int t = sv + 1; t < 4; t++)
-                b.te[6LL * c + pair_slot(sv, t)] = SB.hval[S.cslot[e][cand_of(t, sv)]];
-        }
-        if (sv <= 1 && (b.tf || b.ft)) {
-            const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
-            for (int o = o_lo; o <= o_hi; o++) {
-                const int ko = cand_of(o, sv);
-                const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
-                const unsigned long long mf =
-                    S.hmask[S.cslot[e][ka]] & S.hmask[S.cslot[e][kb]];
-                const int j1 = ctz64(mf);
-                int of = o;
-                if (j1 != pos) {
-                    int x, y;
-                    face_others(w, sv, o, x, y);
-                    of = omitted_slot(S.tv[rs + j1], v, x, y);
-                }
-                const long long q = 4LL * S.cell[rs + j1] + (3 - of);
-                const int fid = rank_of(b.frank, q);
-                if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                if (j1 == pos && b.ft) {
-                    const unsigned long long m2 = mf & (mf - 1);
-                    b.ft[2LL * fid + 1] = m2 ? S.cell[rs + ctz64(m2)] : -1;
-                }
-            }
         }
     }
 }
@@ -607,7 +675,8 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
 // occurrences, so scanning the 6T edge-occurrence slots in order visits the
 // edges in id order: a slot holding a first occurrence contributes the ET
 // and EF row lengths k_star_a left there and deg(a) + deg(b) - 2 for EE.
-constexpr int kEdgeTile = 2048;   // slots per tile, 8 per thread
+constexpr int kEdgeThreads = 256;
+constexpr int kEdgeTile = 8 * kEdgeThreads;   // slots per tile, 8 per thread
 
 struct EdgeOffsets {
     const uint32_t *eflag;
@@ -641,7 +710,7 @@ __device__ __forceinline__ void slot_counts(const EdgeOffsets &p, long long s, i
 
 __device__ __forceinline__ void block_scan3(long long x[3], long long excl[3], long long tot[3])
 {
-    __shared__ long long sm[3][kThreads / 32 + 1];
+    __shared__ long long sm[3][kEdgeThreads / 32 + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -658,22 +727,22 @@ __device__ __forceinline__ void block_scan3(long long x[3], long long excl[3], l
     if (warp == 0) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const long long w = lane < kThreads / 32 ? sm[q][lane] : 0;
+            const long long w = lane < kEdgeThreads / 32 ? sm[q][lane] : 0;
             long long wi = w;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const long long y = __shfl_up_sync(0xffffffffu, wi, o);
                 if (lane >= o) wi += y;
             }
-            if (lane < kThreads / 32) sm[q][lane] = wi - w;
-            if (lane == kThreads / 32 - 1) sm[q][kThreads / 32] = wi;
+            if (lane < kEdgeThreads / 32) sm[q][lane] = wi - w;
+            if (lane == kEdgeThreads / 32 - 1) sm[q][kEdgeThreads / 32] = wi;
         }
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 3; q++) {
         excl[q] += sm[q][warp];
-        tot[q] = sm[q][kThreads / 32];
+        tot[q] = sm[q][kEdgeThreads / 32];
     }
     __syncthreads();
 }
@@ -684,7 +753,7 @@ __device__ __forceinline__ uint32_t slot_bits8(const EdgeOffsets &p, long long s
     return s0 < p.n_slots ? (p.eflag[s0 >> 5] >> (s0 & 31)) & 0xffu : 0u;
 }
 
-__global__ void __launch_bounds__(kThreads) k_edge_offsets_reduce(EdgeOffsets p)
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_reduce(EdgeOffsets p)
 {
     const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
     long long x[3] = {0, 0, 0};
@@ -743,7 +812,7 @@ __global__ void __launch_bounds__(1024) k_edge_offsets_partials(EdgeOffsets p, i
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_edge_offsets_down(EdgeOffsets p, const uint2 *erank)
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets p, const uint2 *erank)
 {
     const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
     long long x[3] = {0, 0, 0};
@@ -832,7 +901,7 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
     const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
     if (tiles > 0) {
         Launch L("k_edge_offsets_reduce", s);
-        k_edge_offsets_reduce<<<(unsigned)tiles, kThreads, 0, s>>>(p);
+        k_edge_offsets_reduce<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p);
     }
     {
         Launch L("k_edge_offsets_partials", s);
@@ -840,7 +909,7 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
     }
     if (tiles > 0) {
         Launch L("k_edge_offsets_down", s);
-        k_edge_offsets_down<<<(unsigned)tiles, kThreads, 0, s>>>(p, erank);
+        k_edge_offsets_down<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p, erank);
     }
 }
 
