@@ -43,6 +43,14 @@ sys.path.insert(0, ROOT)
 METRIC = "Mtets/s (13 relations + crit. points), batched vs per-mesh on 1 GB300; p99 ms"
 UNIT = "Mtets/s"
 WORKLOAD = "kuhn64_coned20_irregular"
+# --workload: the irregular single mesh (the headline) or the 128^3 large mesh
+WORKLOADS = {"irregular": "kuhn64_coned20_irregular", "large": "kuhn128_permuted_large"}
+
+
+def load_workload(key: str):
+    from tetragpu_gb300 import meshgen
+    return WORKLOADS[key], (meshgen.workload_irregular() if key == "irregular"
+                            else meshgen.workload_large())
 ROOFLINE_KERNEL = "k_star_b"
 # CPU sample for the baseline legs: cells [0, SAMPLE_CELLS) of the same mesh
 # (a valid mesh itself), run through the oracle.
@@ -82,7 +90,7 @@ class Clocks:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -134,20 +142,22 @@ def output_bytes(counts: dict, totals: dict) -> int:
 
 def kernel_bytes(name: str, c: dict, tot: dict) -> int:
     """One-touch bytes of one kernel's inputs and outputs (each array read or
-    written once), per launch."""
+    written once), per launch.  k_star_b reads VT (4 B per entry), the sorted
+    TV (16 B per cell), pass A's three candidate masks (24 B per VT entry),
+    VT / VV offsets, the edge and face rank words and the ET / EF offsets; it
+    writes VV and the id-sorted incident edges (4 B each per VV entry), TE,
+    TF, FT's second cell, ET and EF."""
     V, E, F, T = c["V"], c["E"], c["F"], c["T"]
     if name == "k_star_b":
-        reads = 16 * T + 16 * T + 8 * (V + 1) * 2 + 4 * 2 * E + 8 * 2 * E + (10 * T) // 8 \
-            + 4 * (10 * T) // 32
-        writes = 4 * 2 * E + 8 * E + 24 * T + 16 * T + 12 * F + 8 * F + 12 * E + 4 * F + 4 * T
+        reads = 4 * 4 * T + 16 * T + 24 * 4 * T + 8 * (V + 1) * 2 + 8 * ((6 * T + 31) // 32) \
+            + 8 * ((4 * T + 31) // 32) + 8 * (E + 1) * 2
+        writes = 4 * 2 * E * 2 + 4 * 6 * T + 4 * 4 * T + 4 * F + 4 * tot["ET"] + 4 * tot["EF"]
         return reads + writes
     if name == "k_star_a":
-        return 16 * T + 16 * T + 8 * (V + 1) + 12 * 2 * E + 4 * V + (10 * T) // 8
+        return 4 * 4 * T + 16 * T + 8 * (V + 1) + 24 * 4 * T + 4 * V + 2 * 6 * T \
+            + 2 * 4 * ((4 * T + 31) // 32) + 4 * ((6 * T + 31) // 32)
     if name == "k_ee_fill":
         return 8 * E + 4 * 2 * E + 8 * (E + 1) + 8 * (V + 1) + 4 * tot["EE"]
-    if name == "k_star_c":
-        return 16 * T + 16 * T + 8 * (V + 1) + 16 * 2 * E + 4 * 2 * E + 8 * (E + 1) * 2 \
-            + 4 * tot["ET"] + 4 * tot["EF"]
     raise KeyError(name)
 
 
@@ -197,14 +207,14 @@ def cpu_sample(mesh):
     return tv, mesh.n_verts, mesh.field
 
 
-def cpu_baseline(mesh) -> dict:
+def cpu_baseline(mesh, workload: str = WORKLOAD) -> dict:
     from oracle import oracle as O
     O.build()
     tv, nv, field = cpu_sample(mesh)
     times = _cpu_sample_worker((tv, nv, field, 2))
     t = min(times)
     return {"value": round(tv.shape[0] / t / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"cells [0, {tv.shape[0]}) of the {WORKLOAD} mesh, all 13 relations + "
+            "sample": f"cells [0, {tv.shape[0]}) of the {workload} mesh, all 13 relations + "
                       f"critical points, single thread, best of 2 ({t:.2f} s)"}
 
 
@@ -213,9 +223,8 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import oracle as O
-    from tetragpu_gb300 import meshgen
     O.build()
-    mesh = meshgen.workload_irregular()
+    workload, mesh = load_workload(args.workload)
     tv, nv, field = cpu_sample(mesh)
     cores = os.cpu_count() or 1
     # warm-up + timed steps in every worker process, all cores busy at once
@@ -232,10 +241,10 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * tmax / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells_per_step": int(tv.shape[0]),
+        "config": {"workload": workload, "cells_per_step": int(tv.shape[0]),
                    "note": "the reference CPU path (serial) restated in C; one process per core"},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"cells [0, {tv.shape[0]}) of the {WORKLOAD} mesh per step, "
+                         "sample": f"cells [0, {tv.shape[0]}) of the {workload} mesh per step, "
                                    f"{cores} processes in parallel, wall {wall:.1f} s"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -249,10 +258,11 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tetragpu", choices=["tetragpu", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--workload", default="irregular", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -273,7 +283,7 @@ def main():
         _build.build()
     tg.load()
 
-    mesh = meshgen.workload_irregular()
+    workload, mesh = load_workload(args.workload)
     T, V = mesh.n_cells, mesh.n_verts
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
@@ -339,9 +349,6 @@ def main():
     pin_tv = torch.from_numpy(mesh.tv).pin_memory()
     pin_field = torch.from_numpy(mesh.field).pin_memory()
     names = tg.RELATIONS[1:]
-    host = {}
-    for n in names:
-        host[n] = (torch.empty(totals.get(n, 0) if n in totals else 0, dtype=torch.int32).pin_memory())
     fixed_rows = {"TE": (Tc, 6), "EV": (E, 2), "TF": (Tc, 4), "FV": (F, 3), "FE": (F, 3),
                   "FT": (F, 2)}
     csr_rows = {"ET": E, "EF": E, "VT": Vc, "TT": Tc, "FF": F, "EE": E, "VV": Vc}
@@ -364,34 +371,36 @@ def main():
                     g._h, tg.REL[n], h_off[n].data_ptr() if n in h_off else None,
                     h_ent[n].data_ptr() if h_ent[n].numel() else None, s))
 
-    e2e_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    e2e_value = None
+    if args.e2e_steps > 0:
         e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local_rank}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.e2e_steps * T / e2e_s / 1e6
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([e2e_s], device=f"cuda:{local_rank}", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e_value = round(world * args.e2e_steps * T / e2e_s / 1e6, 3)
 
     if rank == 0:
         peak, peak_kind = peaks()
         kb = kernel_bytes(ROOFLINE_KERNEL, counts, totals)
         per_launch_s = (kern_ms / 1e3) / max(kern_n, 1)
         achieved = kb / per_launch_s / 1e9 if kern_n else None
-        traffic = traffic_from_profiles(ROOFLINE_KERNEL, WORKLOAD, T)
+        traffic = traffic_from_profiles(ROOFLINE_KERNEL, workload, T)
         alg = output_bytes(counts, totals)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup),
             "ms_per_step": round(1e3 * t_max / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cells": T, "vertices": V, "edges": E, "faces": F,
+            "config": {"workload": workload, "cells": T, "vertices": V, "edges": E, "faces": F,
                        "relations": "all 13 + critical points", "parallelism": f"replicas{world}",
                        "l2": "flushed before every step (512 MB write)",
                        "path_bytes_per_step": alg,
@@ -399,7 +408,7 @@ def main():
             "gpu_launches": int(launches),
             "wall_s": round(wall, 3),
             "clocks": clk,
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
             "roofline": {"bound": "hbm", "kernel": ROOFLINE_KERNEL,
                          "achieved": round(achieved, 1) if achieved else None, "peak": peak,
@@ -409,7 +418,7 @@ def main():
                          "traffic": traffic},
         }
         if not args.no_cpu_baseline and world >= 1:
-            line["cpu_baseline"] = cpu_baseline(mesh)
+            line["cpu_baseline"] = cpu_baseline(mesh, workload)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
