@@ -224,6 +224,11 @@ struct tg_mesh {
     int64_t V = 0, T = 0, E = -1, F = -1;
     int4 *tvs = nullptr;
     int32_t *vt_win = nullptr;          // VT window table (window_count + 1 entries)
+    // star processing order: vertices by first cell (see tg_star.cu)
+    int32_t *vorder = nullptr;          // [V] vertex at each position (cell-less ones last)
+    int64_t *pofs = nullptr;            // [V + 1] VT offsets in that order
+    int32_t *vtp = nullptr;             // [4T] VT rows in that order
+    int32_t *st_win = nullptr;          // window table over pofs
     Rel rel[14];
     uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
     DevStatus *st = nullptr;    // device
@@ -351,7 +356,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         TRY(tmp.alloc(&frank, nwf + 1));
         TRY(tmp.alloc(&brank, nwf + 1));
         if (need_ecnt) TRY(tmp.alloc(&ecnt, 6 * T, true));
-        TRY(tmp.alloc(&deg, V));
+        TRY(tmp.alloc(&deg, V, true));
         TRY(dalloc(&vv_off, V + 1, s));
         tmp.track(vv_off);  // owned by the VV relation once it is ready
         char *scratch;
@@ -361,7 +366,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         TRY(tmp.alloc(&deg_sq, V + 1));
         uint64_t *emask;  // pass A's candidate masks, pass B's input
         TRY(tmp.alloc(&emask, 3 * NVT));
-        StarA a{vt_off, m->vt_win, vt, m->tvs, V, NVT, deg, ecnt, eflag, fflag, fbnd, m->st, emask};
+        StarA a{m->pofs, m->st_win, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt, eflag, fflag,
+                fbnd, m->st, emask};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));
@@ -442,7 +448,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             if (T == 0) CK(cudaMemsetAsync(ff_off, 0, 8, s));
         }
         StarB b{};
-        b.vt_off = vt_off; b.win = m->vt_win; b.vt = vt; b.tvs = m->tvs; b.V = V; b.nvt = NVT;
+        b.pofs = m->pofs; b.win = m->st_win; b.vorder = m->vorder; b.vtp = m->vtp;
+        b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
@@ -540,6 +547,10 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     for (auto &r : m->rel) free_rel(r, s, true);
     if (m->tvs) cudaFreeAsync(m->tvs, s);
     if (m->vt_win) cudaFreeAsync(m->vt_win, s);
+    if (m->vorder) cudaFreeAsync(m->vorder, s);
+    if (m->pofs) cudaFreeAsync(m->pofs, s);
+    if (m->vtp) cudaFreeAsync(m->vtp, s);
+    if (m->st_win) cudaFreeAsync(m->st_win, s);
     if (m->cadj) cudaFreeAsync(m->cadj, s);
     if (m->st) cudaFreeAsync(m->st, s);
     cudaStreamSynchronize(s);  // no copy into the pinned slots is still in flight
@@ -575,7 +586,7 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     int32_t *vt;
     TRY(dalloc(&vt_off, V + 1, s));
     char *scratch;
-    TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(V) + 256));
+    TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(std::max(V, (4 * T + 31) / 32)) + 256));
     ScanJob job{deg_t, vt_off, V, SCAN_COUNT_I32, 0};
     scan_batch(&job, 1, scratch, s);
     CK(cudaMemsetAsync(deg_t, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
@@ -583,7 +594,32 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     launch_vt_fill(m->tvs, T, vt_off, deg_t, vt, s);
     TRY(dalloc(&m->vt_win, window_count(4 * T, star_window()) + 1, s));
     launch_window_starts(vt_off, V, 4 * T, star_window(), m->vt_win, s);
-    launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, s);
+    // VT row sort, which also marks each vertex's star-order key; then the
+    // star processing order: positions, row lengths, offsets, rows, windows
+    const int64_t nwk = (4 * T + 31) / 32;
+    uint32_t *vflag;
+    uint2 *vrank;
+    int64_t *vkey;
+    int32_t *dcount;
+    TRY(tmp.alloc(&vflag, nwk, true));
+    TRY(tmp.alloc(&vrank, nwk + 1));
+    TRY(tmp.alloc(&vkey, V));
+    TRY(tmp.alloc(&dcount, V, true));
+    launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, m->tvs, vflag, vkey, s);
+    {
+        ScanJob jf{vflag, vrank, nwk, SCAN_POPC_RANK, 0};
+        scan_batch(&jf, 1, scratch, s);
+        TRY(dalloc(&m->vorder, V, s));
+        CK(cudaMemsetAsync(m->vorder, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
+        launch_vorder_place(vt_off, V, vkey, vrank, m->vorder, dcount, s);
+        TRY(dalloc(&m->pofs, V + 1, s));
+        ScanJob jd{dcount, m->pofs, V, SCAN_COUNT_I32, 0};
+        scan_batch(&jd, 1, scratch, s);
+        TRY(dalloc(&m->vtp, 4 * T, s));
+        launch_vtp_fill(m->vorder, m->pofs, V, vt_off, vt, m->vtp, s);
+        TRY(dalloc(&m->st_win, window_count(4 * T, star_window()) + 1, s));
+        launch_window_starts(m->pofs, V, 4 * T, star_window(), m->st_win, s);
+    }
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
     TRY(sync_read(m, s, 0, nullptr, nullptr));

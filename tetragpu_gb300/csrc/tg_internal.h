@@ -73,18 +73,29 @@ int64_t window_count(int64_t n_entries, int win_size);
 void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int win_size,
                           int32_t *win, cudaStream_t s);
 int star_window();  // the window size of the star kernels over VT
-// sort every VT row (tg_star.cu): window-staged, coalesced
+// sort every VT row (tg_star.cu): window-staged, coalesced.  Also marks each
+// vertex's star-order key 4 * (lowest cell) + (slot in it) in vflag (4T bits,
+// zeroed by the caller) and stores it in vkey[v]; rows with no cells are left
+// alone.
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
-                    int64_t nvt, cudaStream_t s);
+                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, cudaStream_t s);
+// Star processing order (vertices by first cell): vorder[pos] = vertex and
+// dcount[pos] = its row length, pos = rank of its key; vtp = VT rows in that
+// order, pofs = its offsets (rows with no cells last, length 0)
+void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
+                         const uint2 *vrank, int32_t *vorder, int32_t *dcount, cudaStream_t s);
+void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
+                     const int32_t *vt, int32_t *vtp, cudaStream_t s);
 
 struct StarA {
-    const int64_t *vt_off;
-    const int32_t *win;        // VT window table
-    const int32_t *vt;
+    const int64_t *pofs;       // VT offsets in star processing order (rows + 1)
+    const int32_t *win;        // window table over pofs
+    const int32_t *vorder;     // vertex at each processing position
+    const int32_t *vtp;        // VT rows in processing order
     const int4 *tvs;
     int64_t V;
     int64_t nvt;               // VT entries (4 * cells)
-    int32_t *deg;              // [V] neighbour counts
+    int32_t *deg;              // [V] neighbour counts (zeroed by the caller)
     uint16_t *ecnt;            // [6T] ET | EF << 8 row lengths at owned edges' first slots
     uint32_t *eflag;           // bit per edge occurrence 6c+j (first occurrences)
     uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
@@ -107,9 +118,10 @@ void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *b
                        cudaStream_t s);
 
 struct StarB {
-    const int64_t *vt_off;
-    const int32_t *win;        // VT window table
-    const int32_t *vt;
+    const int64_t *pofs;       // as in StarA
+    const int32_t *win;
+    const int32_t *vorder;
+    const int32_t *vtp;
     const int4 *tvs;
     int64_t V;
     int64_t nvt;

@@ -147,16 +147,17 @@ __device__ __forceinline__ unsigned long long hk(int rs, int u)
 // Stage the block's window and fill the (vertex, neighbour) table.  Returns
 // false (block-uniformly) when the window cannot be handled here.  win[b] is
 // the first vertex whose row starts at or after entry kWin * b.
-__device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ vt_off,
-                               const int *__restrict__ win, const int *__restrict__ vt,
-                               const int4 *__restrict__ tvs, DevStatus *st, int *deg_zero)
+__device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
+                               const int *__restrict__ win, const int *__restrict__ vorder,
+                               const int *__restrict__ vtp, const int4 *__restrict__ tvs,
+                               DevStatus *st)
 {
     if (threadIdx.x == 0) {
-        const int vlo = win[blockIdx.x], vhi = win[blockIdx.x + 1];
-        S.vlo = vlo;
-        S.vhi = vhi;
-        S.base = vt_off[vlo];
-        S.n = (int)(vt_off[vhi] - S.base);
+        const int plo = win[blockIdx.x], phi = win[blockIdx.x + 1];
+        S.vlo = plo;
+        S.vhi = phi;
+        S.base = pofs[plo];
+        S.n = (int)(pofs[phi] - S.base);
         S.full = 0;
     }
     for (int h = threadIdx.x; h < kHash; h += blockDim.x) {
@@ -168,28 +169,29 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ vt_off,
     if (n > kCap) {
         if (threadIdx.x == 0) {
             atomicOr(&st->flags, ST_HEAVY_STAR);
-            atomicMin(&st->bad_vertex, S.vlo);
+            atomicMin(&st->bad_vertex, vorder[S.vlo]);
         }
         return false;
     }
     const long long base = S.base;
-    for (int v = S.vlo + threadIdx.x; v < S.vhi; v += blockDim.x) {
-        const int rs = (int)(vt_off[v] - base);
-        const int D = (int)(vt_off[v + 1] - vt_off[v]);
-        if (D == 0 && deg_zero) deg_zero[v] = 0;
+    for (int i = S.vlo + threadIdx.x; i < S.vhi; i += blockDim.x) {
+        const int rs = (int)(pofs[i] - base);
+        const int D = (int)(pofs[i + 1] - pofs[i]);
+        if (D == 0) continue;
+        const int v = vorder[i];
         if (D > kMaxStar) {
             atomicOr(&st->flags, ST_HEAVY_STAR);
             atomicMin(&st->bad_vertex, v);
             S.full = 1;
         }
-        for (int i = 0; i < D; i++) {
-            S.vid[rs + i] = v;
-            S.meta[rs + i] = rs | (D << 10);
+        for (int j = 0; j < D; j++) {
+            S.vid[rs + j] = v;
+            S.meta[rs + j] = rs | (D << 10);
         }
-        if (D > 0) S.cnt[rs] = 0;
+        S.cnt[rs] = 0;
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = __ldg(vt + base + e);
+        const int c = __ldg(vtp + base + e);
         S.cell[e] = c;
         S.tv[e] = __ldg(tvs + c);
     }
@@ -232,7 +234,7 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ vt_off,
     if (S.full) {
         if (threadIdx.x == 0) {
             atomicOr(&st->flags, ST_HASH_FULL);
-            atomicMin(&st->bad_vertex, S.vlo);
+            atomicMin(&st->bad_vertex, vorder[S.vlo]);
         }
         return false;
     }
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
     __shared__ Stage S;
     __shared__ int work[3 * kCap];      // first sightings of owned edges (entry << 2 | candidate)
     __shared__ int n_work;
-    if (!stage_and_hash(S, a.vt_off, a.win, a.vt, a.tvs, a.st, a.deg)) return;
+    if (!stage_and_hash(S, a.pofs, a.win, a.vorder, a.vtp, a.tvs, a.st)) return;
     const int n = S.n;
     if (threadIdx.x == 0) n_work = 0;
     __syncthreads();
@@ -354,28 +356,30 @@ __global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
 __device__ void stage_masks(StageM &S, const StarB &b)
 {
     if (threadIdx.x == 0) {
-        const int vlo = b.win[blockIdx.x], vhi = b.win[blockIdx.x + 1];
-        S.vlo = vlo;
-        S.vhi = vhi;
-        S.base = b.vt_off[vlo];
-        S.n = (int)(b.vt_off[vhi] - S.base);
+        const int plo = b.win[blockIdx.x], phi = b.win[blockIdx.x + 1];
+        S.vlo = plo;
+        S.vhi = phi;
+        S.base = b.pofs[plo];
+        S.n = (int)(b.pofs[phi] - S.base);
         S.n_work = 0;
         S.n_owned = 0;
     }
     __syncthreads();
     const int n = S.n;
     const long long base = S.base;
-    for (int v = S.vlo + threadIdx.x; v < S.vhi; v += blockDim.x) {
-        const int rs = (int)(b.vt_off[v] - base);
-        const int D = (int)(b.vt_off[v + 1] - b.vt_off[v]);
-        for (int i = 0; i < D; i++) {
-            S.vid[rs + i] = v;
-            S.meta[rs + i] = rs | (D << 10);
+    for (int i = S.vlo + threadIdx.x; i < S.vhi; i += blockDim.x) {
+        const int rs = (int)(b.pofs[i] - base);
+        const int D = (int)(b.pofs[i + 1] - b.pofs[i]);
+        if (D == 0) continue;
+        const int v = b.vorder[i];
+        for (int j = 0; j < D; j++) {
+            S.vid[rs + j] = v;
+            S.meta[rs + j] = rs | (D << 10);
         }
-        if (D > 0) S.cnt[rs] = 0;
+        S.cnt[rs] = 0;
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = __ldg(b.vt + base + e);
+        const int c = __ldg(b.vtp + base + e);
         S.cell[e] = c;
         S.tv[e] = __ldg(b.tvs + c);
 #pragma unroll
@@ -531,7 +535,7 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
     for (int i = threadIdx.x; i < n_items; i += blockDim.x) {
         if (i < n) {
             const int e = i;
-            const int v = S.vid[e], m = S.meta[e];
+            const int m = S.meta[e];
             const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
             const int4 w = S.tv[e];
             const int c = S.cell[e];
@@ -550,7 +554,7 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
                     if (j1 != pos) {
                         int x, y;
                         face_others(w, sv, o, x, y);
-                        of = omitted_slot(S.tv[rs + j1], v, x, y);
+                        of = omitted_slot(S.tv[rs + j1], S.vid[e], x, y);
                     }
                     const long long q = 4LL * S.cell[rs + j1] + (3 - of);
                     const int fid = rank_of(b.frank, q);
@@ -618,12 +622,24 @@ k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank
 }
 
 // ---------------------------------------------------------------------------
+// Star processing order (see k_vorder_place): vertex v with first cell c in
+// slot k has key 4c + k; its bit in vflag marks it, its rank is v's position.
+__device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_t *vflag,
+                                           int64_t *vkey, int v, int c)
+{
+    const int4 w = __ldg(tvs + c);
+    const long long key = 4LL * c + (w.x == v ? 0 : (w.y == v ? 1 : (w.z == v ? 2 : 3)));
+    vkey[v] = key;
+    atomicOr(vflag + (key >> 5), 1u << (key & 31));
+}
+
 // Sort every VT row ascending.  Rows starting in a window are staged in
 // shared memory and each entry lands at its rank in its row (cells in a row
 // are distinct); windows holding more than kCap entries fall back to an
 // insertion sort per row in global memory.
 __global__ void __launch_bounds__(kThreads)
-k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt)
+k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt,
+          const int4 *__restrict__ tvs, uint32_t *__restrict__ vflag, int64_t *__restrict__ vkey)
 {
     __shared__ int cell[kCap], out[kCap], meta[kCap];
     __shared__ int s_vlo, s_vhi, s_n;
@@ -650,6 +666,7 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
                 }
                 vt[j + 1] = x;
             }
+            if (e > b) mark_first(tvs, vflag, vkey, v, vt[b]);
         }
         return;
     }
@@ -668,6 +685,10 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
     }
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) vt[base + e] = out[e];
+    for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
+        const int64_t b = vt_off[v];
+        if (vt_off[v + 1] > b) mark_first(tvs, vflag, vkey, v, out[b - base]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -870,6 +891,57 @@ k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int w
     for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
 }
 
+// ---------------------------------------------------------------------------
+// Star processing order.  Vertex ids need not carry locality (meshes are
+// often renumbered; the workloads here permute them) while cell order usually
+// does (generators and partitioners emit cells in space-filling order).  The
+// star passes therefore visit vertices by first cell, the head of the sorted
+// VT row, ties by slot: consecutive vertices then share cells, so a block's
+// cell gathers hit L2 and the output sectors of cell- and id-ordered
+// relations it writes are completed by blocks running at the same time.
+// k_vt_sort marks each vertex's key 4 * first cell + slot in a bitmap over
+// the 4T cell slots; the key's rank is the vertex's position.
+__global__ void __launch_bounds__(256)
+k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__restrict__ vkey,
+               const uint2 *__restrict__ vrank, int *__restrict__ vorder, int *__restrict__ dcount)
+{
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const int D = (int)(vt_off[v + 1] - vt_off[v]);
+    if (D == 0) return;
+    const long long key = vkey[v];
+    const uint2 r = __ldg(vrank + (key >> 5));
+    const int pos = (int)r.y + __popc(r.x & ((1u << (key & 31)) - 1u));
+    vorder[pos] = (int)v;
+    dcount[pos] = D;
+}
+
+// VT rows copied into processing order: a warp fetches 32 rows' positions
+// and sources at once, then copies them one after another, lanes across the
+// row
+__global__ void __launch_bounds__(256)
+k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int64_t V,
+           const int64_t *__restrict__ vt_off, const int *__restrict__ vt, int *__restrict__ vtp)
+{
+    const int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const int lane = threadIdx.x & 31;
+    if (r0 >= V) return;  // warp-uniform
+    const int64_t r = r0 + lane;
+    long long dst = 0, src = 0;
+    int D = 0;
+    if (r < V) {
+        dst = pofs[r];
+        D = (int)(pofs[r + 1] - dst);
+        if (D > 0) src = __ldg(vt_off + __ldg(vorder + r));
+    }
+    for (int j = 0; j < 32; j++) {
+        const int Dj = __shfl_sync(0xffffffffu, D, j);
+        const long long dj = __shfl_sync(0xffffffffu, dst, j);
+        const long long sj = __shfl_sync(0xffffffffu, src, j);
+        for (int k = lane; k < Dj; k += 32) vtp[dj + k] = __ldg(vt + sj + k);
+    }
+}
+
 inline unsigned n_windows(int64_t nvt) { return (unsigned)(nvt / kWin + 1); }
 
 }  // namespace
@@ -938,11 +1010,29 @@ void launch_star_b(const StarB &b, cudaStream_t s)
 }
 
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
-                    int64_t nvt, cudaStream_t s)
+                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_vt_sort", s);
-    k_vt_sort<<<n_windows(nvt), kThreads, 0, s>>>(vt_off, win, vt);
+    k_vt_sort<<<n_windows(nvt), kThreads, 0, s>>>(vt_off, win, vt, tvs, vflag, vkey);
+}
+
+
+void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
+                         const uint2 *vrank, int32_t *vorder, int32_t *dcount, cudaStream_t s)
+{
+    if (V == 0) return;
+    Launch L("k_vorder_place", s);
+    k_vorder_place<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vt_off, V, vkey, vrank, vorder,
+                                                                dcount);
+}
+
+void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
+                     const int32_t *vt, int32_t *vtp, cudaStream_t s)
+{
+    if (V == 0) return;
+    Launch L("k_vtp_fill", s);
+    k_vtp_fill<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vorder, pofs, V, vt_off, vt, vtp);
 }
 
 }  // namespace tg
