@@ -43,8 +43,11 @@ sys.path.insert(0, ROOT)
 METRIC = "Mtets/s (13 relations + crit. points), batched vs per-mesh on 1 GB300; p99 ms"
 UNIT = "Mtets/s"
 WORKLOAD = "kuhn64_coned20_irregular"
-# --workload: the irregular single mesh (the headline) or the 128^3 large mesh
-WORKLOADS = {"irregular": "kuhn64_coned20_irregular", "large": "kuhn128_permuted_large"}
+# --workload: the irregular single mesh (the headline), the 128^3 large mesh,
+# or the uneven 512-mesh batch (batched path against the per-mesh loop)
+WORKLOADS = {"irregular": "kuhn64_coned20_irregular", "large": "kuhn128_permuted_large",
+             "batch": "batch512_uneven_2k_400k"}
+DEFAULT_STEPS = {"irregular": 300, "large": 60, "batch": 5}
 
 
 def load_workload(key: str):
@@ -255,17 +258,153 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def main_batch(args, torch, dist, tg, rank, local_rank, world):
+    """The uneven 512-mesh batch: one batched pipeline run (tg_batch_*) per
+    step against the plain per-mesh loop (tg_mesh_* per mesh) over the same
+    device-resident meshes; both arms time the same step (create, all 13
+    relations, critical points, destroy) with CUDA events."""
+    from tetragpu_gb300 import meshgen
+    meshes = meshgen.workload_batch()
+    nc = np.array([m.n_cells for m in meshes], dtype=np.int64)
+    nv = np.array([m.n_verts for m in meshes], dtype=np.int64)
+    c_off = np.concatenate([[0], np.cumsum(nc)])
+    v_off = np.concatenate([[0], np.cumsum(nv)])
+    T, V = int(c_off[-1]), int(v_off[-1])
+    tv_all = np.concatenate([m.tv for m in meshes])
+    f_all = np.concatenate([m.field for m in meshes]).astype(np.float32)
+    dev = f"cuda:{local_rank}"
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    d_tv = torch.from_numpy(tv_all).to(dev)
+    d_f = torch.from_numpy(f_all).to(dev)
+    d_cls = torch.empty(3 * V, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def batch_step():
+        with tg.Batch(d_tv.data_ptr(), nv, n_cells=nc, on_device=True, stream=s) as b:
+            b.extract(tg.ALL_RELATIONS, stream=s)
+            b.critical_points(d_f.data_ptr(), on_device=True, out_ptr=d_cls.data_ptr(), stream=s)
+
+    def loop_step():
+        for i in range(len(meshes)):
+            with tg.Mesh(d_tv.data_ptr() + 16 * int(c_off[i]), int(nv[i]), n_cells=int(nc[i]),
+                         on_device=True, stream=s) as g:
+                g.extract(tg.ALL_RELATIONS, stream=s)
+                g.critical_points(d_f.data_ptr() + 4 * int(v_off[i]), on_device=True,
+                                  out_ptr=d_cls.data_ptr() + 12 * int(v_off[i]), stream=s)
+
+    def timed(fn, k_steps):
+        with torch.cuda.stream(stream):
+            for _ in range(max(3, args.warmup)):
+                fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k_steps)]
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = tg.kernel_launch_count()
+        with torch.cuda.stream(stream):
+            for k in range(k_steps):
+                flush.fill_(k & 0xff)
+                ev[k][0].record(stream)
+                fn()
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return total, tg.kernel_launch_count() - l0
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    t_batch, launches = timed(batch_step, args.steps)
+    clk = clocks.stop()
+    t_loop, loop_launches = timed(loop_step, args.steps)
+    value = world * args.steps * T / t_batch / 1e6
+    loop_value = world * args.steps * T / t_loop / 1e6
+
+    # e2e: host TV and fields in, every relation of the union and the classes
+    # back to host memory, through the batch API
+    pin_tv = torch.from_numpy(tv_all).pin_memory()
+    pin_f = torch.from_numpy(f_all).pin_memory()
+    h_cls = np.empty((V, 3), dtype=np.uint32)
+    h_bufs = {}
+    e2e_value, h2d, d2h = None, pin_tv.numel() * 4 + pin_f.numel() * 4, h_cls.nbytes
+    lib = tg.load()
+    if args.e2e_steps > 0:
+        def e2e_step():
+            with tg.Batch(pin_tv.data_ptr(), nv, n_cells=nc, stream=s) as b:
+                b.extract(tg.ALL_RELATIONS, stream=s)
+                tg._lib.check(lib.tg_batch_critical_points(b._h, pin_f.data_ptr(), tg.FIELD_F32,
+                                                           0, h_cls.ctypes.data, 0, s))
+                u = lib.tg_batch_union(b._h)
+                for n in tg.RELATIONS[1:]:
+                    off, ent = tg._lib.C.c_void_p(), tg._lib.C.c_void_p()
+                    rows, cnt, width = (tg._lib.C.c_int64(), tg._lib.C.c_int64(),
+                                        tg._lib.C.c_int32())
+                    tg._lib.check(lib.tg_get_relation(u, tg.REL[n], tg._lib.C.byref(off),
+                                                      tg._lib.C.byref(ent), tg._lib.C.byref(rows),
+                                                      tg._lib.C.byref(cnt),
+                                                      tg._lib.C.byref(width)))
+                    if n not in h_bufs:
+                        h_bufs[n] = (torch.empty(max(cnt.value, 1), dtype=torch.int32).pin_memory(),
+                                     torch.empty(rows.value + 1, dtype=torch.int64).pin_memory()
+                                     if width.value == 0 else None)
+                    he, ho = h_bufs[n]
+                    tg._lib.check(lib.tg_copy_relation(u, tg.REL[n],
+                                                       ho.data_ptr() if ho is not None else None,
+                                                       he.data_ptr() if cnt.value else None, s))
+        e2e_step()
+        torch.cuda.synchronize()
+        d2h += sum(a.numel() * 4 + (b.numel() * 8 if b is not None else 0)
+                   for a, b in h_bufs.values())
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_value = round(world * args.e2e_steps * T / (time.perf_counter() - t0) / 1e6, 3)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": round(1e3 * t_batch / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["batch"], "meshes": len(meshes), "cells": T,
+                       "vertices": V, "relations": "all 13 + critical points",
+                       "parallelism": f"replicas{world}",
+                       "l2": "flushed before every step (512 MB write)"},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "per_mesh_loop": {"value": round(loop_value, 3), "unit": UNIT,
+                              "ms_per_step": round(1e3 * t_loop / args.steps, 3),
+                              "gpu_launches": int(loop_launches)},
+            "batched_over_loop": round(value / loop_value, 3),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tetragpu", choices=["tetragpu", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--workload", default="irregular", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" else DEFAULT_STEPS[args.workload]
     if args.impl == "reference":
+        if args.workload == "batch":
+            args.workload = "irregular"
         run_reference(args)
         return
 
@@ -283,6 +422,11 @@ def main():
         _build.build()
     tg.load()
 
+    if args.workload == "batch":
+        main_batch(args, torch, dist, tg, rank, local_rank, world)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     workload, mesh = load_workload(args.workload)
     T, V = mesh.n_cells, mesh.n_verts
     stream = torch.cuda.Stream()

@@ -195,6 +195,48 @@ tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int32_t *vv, i
                                      int64_t n_vv_entries, const void *field, int field_type,
                                      uint32_t *classes_out, void *stream);
 
+/* ---- batches of independent meshes ---------------------------------------
+ * Many meshes processed as one: their disjoint union is a mesh, so every
+ * kernel of the path runs once over all of them (no per-mesh launches,
+ * allocations or synchronisations).  A mesh's relations are the union's
+ * restricted to its rows, minus its first vertex / edge / face / cell id, and
+ * are identical to what that mesh alone gives (ids are ranks of first
+ * occurrences in cell order and a mesh's cells are contiguous).  No
+ * counterpart in the reference, which runs one mesh per process. */
+typedef struct tg_batch tg_batch;
+
+/* tv: the meshes' cells back to back, int32 [sum n_cells x 4], each mesh
+ * with its own vertex ids 0 .. n_verts[i] - 1 (an id outside that range is
+ * TG_ERR_INVALID_MESH).  n_cells / n_verts: host arrays of n_meshes. */
+tg_status tg_batch_create(const int32_t *tv, const int64_t *n_cells, const int64_t *n_verts,
+                          int64_t n_meshes, int tv_on_device, void *stream, tg_batch **out);
+tg_status tg_batch_destroy(tg_batch *batch);
+/* tg_extract over the whole batch. */
+tg_status tg_batch_extract(tg_batch *batch, uint32_t relation_mask, uint32_t options,
+                           void *stream);
+/* tg_critical_points over the whole batch: field holds every mesh's values
+ * back to back (sum n_verts), classes_out uint32 [sum n_verts x 3]. */
+tg_status tg_batch_critical_points(tg_batch *batch, const void *field, int field_type,
+                                   int field_on_device, uint32_t *classes_out,
+                                   int out_on_device, void *stream);
+/* Counts of mesh i (E and F once extracted, else -1).  Synchronous on first
+ * use after an extraction. */
+tg_status tg_batch_mesh_counts(tg_batch *batch, int64_t i, int64_t *n_verts, int64_t *n_edges,
+                               int64_t *n_faces, int64_t *n_cells);
+/* Mesh i's relation with that mesh's own ids, copied to host memory:
+ * offsets_out (CSR: rows + 1, starting at 0; NULL for fixed width or not
+ * wanted) and entries_out.  Sizes from tg_batch_relation_size.  Synchronous. */
+tg_status tg_batch_relation_size(tg_batch *batch, int64_t i, int relation, int64_t *rows,
+                                 int64_t *entries, int32_t *width);
+tg_status tg_batch_copy_relation(tg_batch *batch, int64_t i, int relation, int64_t *offsets_out,
+                                 int32_t *entries_out, void *stream);
+/* The union mesh (ids of the whole batch), e.g. for tg_get_relation. */
+tg_mesh *tg_batch_union(tg_batch *batch);
+/* First vertex, edge, face and cell id of mesh i in the union (E and F once
+ * extracted). */
+tg_status tg_batch_mesh_offsets(tg_batch *batch, int64_t i, int64_t *vert0, int64_t *edge0,
+                                int64_t *face0, int64_t *cell0);
+
 /* Time every launch of one kernel (by name, e.g. "k_star_b") with CUDA
  * events recorded on the stream it is launched on; NULL or "" turns timing
  * off.  For measurement tools; the reference's analogue is its Timer class

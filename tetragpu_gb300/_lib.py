@@ -70,6 +70,15 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_kernel_launch_count": (i64, []),
         "tg_profile_kernel": (C.c_int, [C.c_char_p]),
         "tg_profile_read": (C.c_int, [P(C.c_double), P(i64), C.c_int]),
+        "tg_batch_create": (C.c_int, [vp, vp, vp, i64, C.c_int, vp, P(vp)]),
+        "tg_batch_destroy": (C.c_int, [vp]),
+        "tg_batch_extract": (C.c_int, [vp, u32, u32, vp]),
+        "tg_batch_critical_points": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]),
+        "tg_batch_mesh_counts": (C.c_int, [vp, i64, P(i64), P(i64), P(i64), P(i64)]),
+        "tg_batch_mesh_offsets": (C.c_int, [vp, i64, P(i64), P(i64), P(i64), P(i64)]),
+        "tg_batch_relation_size": (C.c_int, [vp, i64, C.c_int, P(i64), P(i64), P(i32)]),
+        "tg_batch_copy_relation": (C.c_int, [vp, i64, C.c_int, vp, vp, vp]),
+        "tg_batch_union": (vp, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -196,6 +205,119 @@ class Mesh:
 
     def device_bytes(self) -> int:
         return int(self._lib.tg_mesh_device_bytes(self._h))
+
+
+class Batch:
+    """Independent meshes processed as one (their disjoint union).
+
+    ``tvs`` is a list of int32 [n_cells_i, 4] arrays, each with its own
+    vertex ids 0 .. n_verts[i] - 1; or, with ``n_cells`` given, every cell
+    back to back as one host int32 array, a host pointer (int), or with
+    ``on_device=True`` a device pointer.
+    """
+
+    def __init__(self, tvs, n_verts, n_cells=None, on_device: bool = False, stream=None):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        nv = np.ascontiguousarray(n_verts, dtype=np.int64)
+        if on_device or n_cells is not None:
+            # all cells back to back: a device pointer, a host pointer, or a
+            # host int32 array
+            nc = np.ascontiguousarray(n_cells, dtype=np.int64)
+            if isinstance(tvs, int):
+                ptr = tvs
+                keep = None
+            else:
+                keep = np.ascontiguousarray(tvs, dtype=np.int32)
+                ptr = keep.ctypes.data if keep.size else None
+        else:
+            parts = [np.ascontiguousarray(t, dtype=np.int32).reshape(-1, 4) for t in tvs]
+            nc = np.array([p.shape[0] for p in parts], dtype=np.int64)
+            keep = np.concatenate(parts) if parts else np.zeros((0, 4), np.int32)
+            ptr = keep.ctypes.data if keep.size else None
+        assert nc.shape == nv.shape
+        self.n_meshes = int(nv.shape[0])
+        self.n_verts = nv
+        self.n_cells = nc
+        check(lib.tg_batch_create(ptr, nc.ctypes.data, nv.ctypes.data, self.n_meshes,
+                                  int(bool(on_device)), _stream(stream), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            self._lib.tg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def extract(self, relations=ALL_RELATIONS, options: int = 0, stream=None):
+        mask = relations if isinstance(relations, int) else mask_of(relations)
+        check(self._lib.tg_batch_extract(self._h, mask, options, _stream(stream)))
+        return self
+
+    def counts(self, i: int) -> tuple:
+        v, e, f, t = (C.c_int64() for _ in range(4))
+        check(self._lib.tg_batch_mesh_counts(self._h, i, C.byref(v), C.byref(e), C.byref(f),
+                                             C.byref(t)))
+        return v.value, e.value, f.value, t.value
+
+    def offsets(self, i: int) -> tuple:
+        """First (vertex, edge, face, cell) id of mesh i in the union."""
+        v, e, f, t = (C.c_int64() for _ in range(4))
+        check(self._lib.tg_batch_mesh_offsets(self._h, i, C.byref(v), C.byref(e), C.byref(f),
+                                              C.byref(t)))
+        return v.value, e.value, f.value, t.value
+
+    def relation(self, i: int, name: str, stream=None):
+        """Mesh i's relation with its own ids: [rows, width], or (offsets, entries)."""
+        r = REL[name]
+        rows, n, width = C.c_int64(), C.c_int64(), C.c_int32()
+        check(self._lib.tg_batch_relation_size(self._h, i, r, C.byref(rows), C.byref(n),
+                                               C.byref(width)))
+        ent = np.empty(n.value, dtype=np.int32)
+        if width.value > 0:
+            check(self._lib.tg_batch_copy_relation(self._h, i, r, None,
+                                                   ent.ctypes.data if ent.size else None,
+                                                   _stream(stream)))
+            return ent.reshape(rows.value, width.value)
+        off = np.empty(rows.value + 1, dtype=np.int64)
+        check(self._lib.tg_batch_copy_relation(self._h, i, r, off.ctypes.data,
+                                               ent.ctypes.data if ent.size else None,
+                                               _stream(stream)))
+        return off, ent
+
+    def critical_points(self, field, on_device: bool = False, out_ptr: int | None = None,
+                        field_type: int | None = None, stream=None):
+        """All meshes' classes back to back, uint32 [sum n_verts, 3]."""
+        if on_device:
+            fptr = int(field)
+            ftype = FIELD_F32 if field_type is None else field_type
+        else:
+            arr = np.ascontiguousarray(field)
+            if arr.dtype == np.float64:
+                ftype = FIELD_F64
+            else:
+                arr = arr.astype(np.float32, copy=False)
+                ftype = FIELD_F32
+            fptr = arr.ctypes.data
+        if out_ptr is not None:
+            check(self._lib.tg_batch_critical_points(self._h, fptr, ftype, int(bool(on_device)),
+                                                     int(out_ptr), 1, _stream(stream)))
+            return None
+        out = np.empty((int(self.n_verts.sum()), 3), dtype=np.uint32)
+        check(self._lib.tg_batch_critical_points(self._h, fptr, ftype, int(bool(on_device)),
+                                                 out.ctypes.data, 0, _stream(stream)))
+        return out
 
 
 def kernel_launch_count() -> int:

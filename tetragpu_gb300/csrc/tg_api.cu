@@ -229,6 +229,11 @@ struct tg_mesh {
     int64_t *pofs = nullptr;            // [V + 1] VT offsets in that order
     int32_t *vtp = nullptr;             // [4T] VT rows in that order
     int32_t *st_win = nullptr;          // window table over pofs
+    // segments of cells (the meshes of a batch): cell starts, and after each
+    // extraction their first edge and face ids (device, n_seg + 1 each)
+    int64_t n_seg = 0;
+    int64_t *seg_c = nullptr;
+    int64_t *seg_ef = nullptr;
     Rel rel[14];
     uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
     DevStatus *st = nullptr;    // device
@@ -396,6 +401,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         const int64_t sum_deg_sq = m->sz_host[4];
         m->E = E;
         m->F = F;
+        if (m->seg_c) launch_seg_ranks(m->seg_c, m->n_seg, erank, frank, m->seg_ef, s);
         int64_t *et_off = nullptr, *ef_off = nullptr, *ee_off = nullptr;
         if (mask & TG_ET) TRY(dalloc(&et_off, E + 1, s));
         if (mask & TG_EF) TRY(dalloc(&ef_off, E + 1, s));
@@ -551,6 +557,8 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     if (m->pofs) cudaFreeAsync(m->pofs, s);
     if (m->vtp) cudaFreeAsync(m->vtp, s);
     if (m->st_win) cudaFreeAsync(m->st_win, s);
+    if (m->seg_c) cudaFreeAsync(m->seg_c, s);
+    if (m->seg_ef) cudaFreeAsync(m->seg_ef, s);
     if (m->cadj) cudaFreeAsync(m->cadj, s);
     if (m->st) cudaFreeAsync(m->st, s);
     cudaStreamSynchronize(s);  // no copy into the pinned slots is still in flight
@@ -841,3 +849,20 @@ int64_t tg_mesh_device_bytes(const tg_mesh *m)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// internal: segments (tg_batch.cu)
+tg_status tg::mesh_set_segments(tg_mesh *m, const int64_t *seg_c_host, int64_t n, cudaStream_t s)
+{
+    if (m->seg_c) cudaFreeAsync(m->seg_c, s);
+    if (m->seg_ef) cudaFreeAsync(m->seg_ef, s);
+    m->seg_c = m->seg_ef = nullptr;
+    m->n_seg = n;
+    TRY(dalloc(&m->seg_c, n + 1, s));
+    TRY(dalloc(&m->seg_ef, 2 * (n + 1), s));
+    CK(cudaMemcpyAsync(m->seg_c, seg_c_host, (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the host array may go away
+    return TG_OK;
+}
+
+const int64_t *tg::mesh_segment_ids(const tg_mesh *m) { return m->seg_ef; }

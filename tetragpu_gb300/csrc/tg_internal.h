@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "tetragpu.h"
+
 namespace tg {
 
 // Device-side status word, written by kernels with atomics, read back by the
@@ -104,6 +106,10 @@ struct StarA {
     uint64_t *emask;           // [3][nvt] star positions holding each entry's candidates
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
+// seg_ef[i] = first edge id and seg_ef[n + 1 + i] = first face id of the
+// cells from seg_c[i] on (i = 0 .. n; seg_c[n] = T gives the totals)
+void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const uint2 *frank,
+                      int64_t *seg_ef, cudaStream_t s);
 
 // ET / EF / EE offsets in edge-id order from one scan over the 6T edge slots
 size_t edge_offsets_scratch_bytes(int64_t n_slots);
@@ -168,6 +174,11 @@ void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64
 
 // the message tg_last_error_string returns on this thread
 void set_last_error(const char *msg);
+// Cell segments of a mesh (the meshes of a batch, tg_batch.cu): seg_c_host
+// holds n + 1 cell starts; each extraction then fills n + 1 first edge ids
+// followed by n + 1 first face ids (device, read by mesh_segment_ids).
+tg_status mesh_set_segments(tg_mesh *m, const int64_t *seg_c_host, int64_t n, cudaStream_t s);
+const int64_t *mesh_segment_ids(const tg_mesh *m);
 
 // launch accounting and optional CUDA-event timing of one named kernel
 void count_launch(int n = 1);

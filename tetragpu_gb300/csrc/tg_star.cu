@@ -942,6 +942,19 @@ k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int
     }
 }
 
+// First edge and face id of each segment of cells (a mesh of a batch):
+// ids are ranks of first occurrences in cell order, so segment i's ids start
+// at the rank of its first cell's first occurrence slot.
+__global__ void __launch_bounds__(256)
+k_seg_ranks(const int64_t *__restrict__ seg_c, int64_t n, const uint2 *__restrict__ erank,
+            const uint2 *__restrict__ frank, int64_t *__restrict__ seg_ef)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    seg_ef[i] = rank_of(erank, 6LL * seg_c[i]);
+    seg_ef[n + 1 + i] = rank_of(frank, 4LL * seg_c[i]);
+}
+
 inline unsigned n_windows(int64_t nvt) { return (unsigned)(nvt / kWin + 1); }
 
 }  // namespace
@@ -1033,6 +1046,14 @@ void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, cons
     if (V == 0) return;
     Launch L("k_vtp_fill", s);
     k_vtp_fill<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vorder, pofs, V, vt_off, vt, vtp);
+}
+
+
+void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const uint2 *frank,
+                      int64_t *seg_ef, cudaStream_t s)
+{
+    Launch L("k_seg_ranks", s);
+    k_seg_ranks<<<(unsigned)((n + 1 + 255) / 256), 256, 0, s>>>(seg_c, n, erank, frank, seg_ef);
 }
 
 }  // namespace tg
