@@ -104,6 +104,8 @@ const char *tg_last_error_string(void);
 tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts,
                          int tv_on_device, void *stream, tg_mesh **out);
 
+/* Frees the mesh's device memory, ordered on the stream of its last call and
+ * waiting for that stream: destroy a mesh before the stream it last used. */
 tg_status tg_mesh_destroy(tg_mesh *mesh);
 
 /* Extract every relation whose bit is set (plus what they depend on) and keep
@@ -236,6 +238,62 @@ tg_mesh *tg_batch_union(tg_batch *batch);
  * extracted). */
 tg_status tg_batch_mesh_offsets(tg_batch *batch, int64_t i, int64_t *vert0, int64_t *edge0,
                                 int64_t *face0, int64_t *cell0);
+
+/* ---- serving -------------------------------------------------------------
+ * A request loop over one device: new meshes (with a field) and new fields on
+ * meshes already resident.  Worker slots (a thread and a CUDA stream each) run
+ * concurrently; when a slot frees, the new-mesh requests waiting at the head
+ * of the queue are merged into one batch (tg_batch_*) up to batch_cells cells
+ * and up to the device-memory budget, so requests that arrive while others are
+ * on the GPU join the next batch and overlap on the device.  Meshes stay
+ * resident (their relations and link adjacency) for later fields; when memory
+ * runs short, idle resident batches are evicted least-recently-used first and
+ * a later field on an evicted mesh rebuilds it from the host copy of its TV.
+ * Results are identical to the mesh processed alone.  No counterpart in the
+ * reference. */
+typedef struct tg_server tg_server;
+typedef struct {
+    int32_t n_slots;          /* concurrent work slots; 0 = 4 */
+    int64_t hbm_budget_bytes; /* device memory for resident meshes and work in flight; 0 = 150e9 */
+    int64_t batch_cells;      /* most cells merged into one batch; 0 = 4,194,304 */
+    uint32_t relation_mask;   /* relations extracted for every new mesh (VV always added) */
+} tg_server_config;
+typedef struct {
+    int64_t submitted, completed, failed;
+    int64_t batches;          /* pipeline runs for new meshes */
+    int64_t meshes_built;     /* meshes created, rebuilt ones included */
+    int64_t evictions;        /* resident batches evicted for memory */
+    int64_t resident_meshes, resident_bytes, peak_bytes;
+} tg_server_stats;
+
+/* device: CUDA device index; cfg may be NULL (defaults). */
+tg_status tg_server_create(int device, const tg_server_config *cfg, tg_server **out);
+/* Waits for every request in flight, then frees everything. */
+tg_status tg_server_destroy(tg_server *server);
+/* A new mesh and a field on it.  TV (int32 [n_cells x 4], host) and the field
+ * (n_verts values, host) are copied before returning.  request_id names the
+ * request for tg_server_wait; mesh_id names the resident mesh. */
+tg_status tg_server_submit_mesh(tg_server *server, const int32_t *tv, int64_t n_cells,
+                                int64_t n_verts, const void *field, int field_type,
+                                int64_t *request_id, int64_t *mesh_id);
+/* A new field on a resident mesh (copied before returning). */
+tg_status tg_server_submit_field(tg_server *server, int64_t mesh_id, const void *field,
+                                 int field_type, int64_t *request_id);
+/* Waits for a request (timeout_ms < 0: no limit; TG_ERR_TIMEOUT when it runs
+ * out) and hands back its classes (host uint32 [n_verts x 3], may be NULL)
+ * and its latency from submission to completion.  A request can be waited
+ * for once; its record is then dropped. */
+tg_status tg_server_wait(tg_server *server, int64_t request_id, int64_t timeout_ms,
+                         uint32_t *classes_out, double *latency_ms);
+/* Relation of a resident mesh with its own ids (extracted if needed), like
+ * tg_batch_relation_size / tg_batch_copy_relation.  Synchronous. */
+tg_status tg_server_relation_size(tg_server *server, int64_t mesh_id, int relation,
+                                  int64_t *rows, int64_t *entries, int32_t *width);
+tg_status tg_server_copy_relation(tg_server *server, int64_t mesh_id, int relation,
+                                  int64_t *offsets_out, int32_t *entries_out);
+/* The mesh is no longer needed; its memory goes once its batch is unused. */
+tg_status tg_server_release_mesh(tg_server *server, int64_t mesh_id);
+tg_status tg_server_get_stats(tg_server *server, tg_server_stats *out);
 
 /* Time every launch of one kernel (by name, e.g. "k_star_b") with CUDA
  * events recorded on the stream it is launched on; NULL or "" turns timing

@@ -79,6 +79,15 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_batch_relation_size": (C.c_int, [vp, i64, C.c_int, P(i64), P(i64), P(i32)]),
         "tg_batch_copy_relation": (C.c_int, [vp, i64, C.c_int, vp, vp, vp]),
         "tg_batch_union": (vp, [vp]),
+        "tg_server_create": (C.c_int, [C.c_int, vp, P(vp)]),
+        "tg_server_destroy": (C.c_int, [vp]),
+        "tg_server_submit_mesh": (C.c_int, [vp, vp, i64, i64, vp, C.c_int, P(i64), P(i64)]),
+        "tg_server_submit_field": (C.c_int, [vp, i64, vp, C.c_int, P(i64)]),
+        "tg_server_wait": (C.c_int, [vp, i64, i64, vp, P(C.c_double)]),
+        "tg_server_relation_size": (C.c_int, [vp, i64, C.c_int, P(i64), P(i64), P(i32)]),
+        "tg_server_copy_relation": (C.c_int, [vp, i64, C.c_int, vp, vp]),
+        "tg_server_release_mesh": (C.c_int, [vp, i64]),
+        "tg_server_get_stats": (C.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -318,6 +327,109 @@ class Batch:
         check(self._lib.tg_batch_critical_points(self._h, fptr, ftype, int(bool(on_device)),
                                                  out.ctypes.data, 0, _stream(stream)))
         return out
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("n_slots", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+                ("batch_cells", C.c_int64), ("relation_mask", C.c_uint32)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "batches",
+                                         "meshes_built", "evictions", "resident_meshes",
+                                         "resident_bytes", "peak_bytes")]
+
+
+class Server:
+    """Request loop with continuous batching on one device (tg_server_*)."""
+
+    def __init__(self, device: int = 0, n_slots: int = 4, hbm_budget_bytes: int = 150 * 10**9,
+                 batch_cells: int = 4 * 1024 * 1024, relations=ALL_RELATIONS):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        mask = relations if isinstance(relations, int) else mask_of(relations)
+        cfg = _ServerConfig(n_slots, hbm_budget_bytes, batch_cells, mask)
+        check(lib.tg_server_create(device, C.byref(cfg), C.byref(self._h)))
+        self._nv = {}
+
+    def close(self):
+        if self._h:
+            self._lib.tg_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _field(field):
+        arr = np.ascontiguousarray(field)
+        if arr.dtype != np.float64:
+            arr = arr.astype(np.float32, copy=False)
+        return arr, (FIELD_F64 if arr.dtype == np.float64 else FIELD_F32)
+
+    def submit_mesh(self, tv, n_verts: int, field) -> tuple:
+        """(request id, mesh id); TV and field are copied before returning."""
+        tv = np.ascontiguousarray(tv, dtype=np.int32).reshape(-1, 4)
+        f, ft = self._field(field)
+        rid, mid = C.c_int64(), C.c_int64()
+        check(self._lib.tg_server_submit_mesh(self._h, tv.ctypes.data if tv.size else None,
+                                              tv.shape[0], int(n_verts),
+                                              f.ctypes.data if f.size else None, ft,
+                                              C.byref(rid), C.byref(mid)))
+        self._nv[rid.value] = int(n_verts)
+        self._nv[("mesh", mid.value)] = int(n_verts)
+        return rid.value, mid.value
+
+    def submit_field(self, mesh_id: int, field) -> int:
+        f, ft = self._field(field)
+        rid = C.c_int64()
+        check(self._lib.tg_server_submit_field(self._h, mesh_id, f.ctypes.data if f.size else None,
+                                               ft, C.byref(rid)))
+        self._nv[rid.value] = self._nv.get(("mesh", mesh_id), f.shape[0])
+        return rid.value
+
+    def wait(self, request_id: int, timeout_ms: int = -1) -> tuple:
+        """(classes uint32 [V, 3], latency ms)."""
+        nv = self._nv.pop(request_id, 0)
+        out = np.empty((nv, 3), dtype=np.uint32)
+        lat = C.c_double()
+        check(self._lib.tg_server_wait(self._h, request_id, timeout_ms,
+                                       out.ctypes.data if out.size else None, C.byref(lat)))
+        return out, lat.value
+
+    def relation(self, mesh_id: int, name: str):
+        r = REL[name]
+        rows, n, width = C.c_int64(), C.c_int64(), C.c_int32()
+        check(self._lib.tg_server_relation_size(self._h, mesh_id, r, C.byref(rows), C.byref(n),
+                                                C.byref(width)))
+        ent = np.empty(n.value, dtype=np.int32)
+        if width.value > 0:
+            check(self._lib.tg_server_copy_relation(self._h, mesh_id, r, None,
+                                                    ent.ctypes.data if ent.size else None))
+            return ent.reshape(rows.value, width.value)
+        off = np.empty(rows.value + 1, dtype=np.int64)
+        check(self._lib.tg_server_copy_relation(self._h, mesh_id, r, off.ctypes.data,
+                                                ent.ctypes.data if ent.size else None))
+        return off, ent
+
+    def release(self, mesh_id: int):
+        check(self._lib.tg_server_release_mesh(self._h, mesh_id))
+        self._nv.pop(("mesh", mesh_id), None)
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        check(self._lib.tg_server_get_stats(self._h, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in _ServerStats._fields_}
 
 
 def kernel_launch_count() -> int:

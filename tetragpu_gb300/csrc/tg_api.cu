@@ -533,6 +533,49 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
 
 }  // namespace
 
+tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const void *field,
+                                   int field_type, int field_on_device, uint32_t *classes_out,
+                                   int out_on_device, cudaStream_t s)
+{
+    if (!m || !field || !classes_out) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (field_type != TG_FIELD_F32 && field_type != TG_FIELD_F64)
+        return fail(TG_ERR_INVALID_ARGUMENT, "field_type must be TG_FIELD_F32 or TG_FIELD_F64");
+    if (v0 < 0 || nv < 0 || v0 + nv > m->V) return fail(TG_ERR_INVALID_ARGUMENT, "bad vertex range");
+    m->last_stream = s;
+    if (!m->rel[TG_REL_VV].ready) TRY(tg_extract(m, TG_VV, 0, s));
+    const int64_t V = m->V;
+    const Rel &vv = m->rel[TG_REL_VV];
+    if (!m->cadj) {
+        TRY(reset_status(m, s));
+        TRY(dalloc(&m->cadj, vv.entries, s));
+        int32_t *vv_win;
+        TRY(dalloc(&vv_win, window_count(vv.entries, crit_window()) + 1, s));
+        launch_window_starts(vv.off, V, vv.entries, crit_window(), vv_win, s);
+        // VV rows longer than the adjacency masks were already rejected by
+        // tg_extract (star pass A flags them), so no status read-back here
+        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st, s);
+        cudaFreeAsync(vv_win, s);
+    }
+    Temps tmp(s);
+    const size_t esz = field_type == TG_FIELD_F64 ? 8 : 4;
+    const void *f = field;
+    if (!field_on_device) {
+        char *d;
+        TRY(tmp.alloc(&d, (int64_t)(nv * esz)));
+        CK(cudaMemcpyAsync(d, field, nv * esz, cudaMemcpyHostToDevice, s));
+        f = d;
+    }
+    uint32_t *out = classes_out;
+    if (!out_on_device) TRY(tmp.alloc(&out, 3 * nv));
+    launch_crit_classify(vv.off, vv.ent, m->cadj, f, field_type, v0, nv, out, s);
+    CK(cudaGetLastError());
+    if (!out_on_device) {
+        CK(cudaMemcpyAsync(classes_out, out, (size_t)nv * 12, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return TG_OK;
+}
+
 extern "C" {
 
 const char *tg_version(void) { return "tetragpu-gb300 1.0 (sm_103a)"; }
@@ -765,43 +808,9 @@ tg_status tg_get_tv(const tg_mesh *m, const int32_t **tv)
 tg_status tg_critical_points(tg_mesh *m, const void *field, int field_type, int field_on_device,
                              uint32_t *classes_out, int out_on_device, void *stream)
 {
-    if (!m || !field || !classes_out) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (field_type != TG_FIELD_F32 && field_type != TG_FIELD_F64)
-        return fail(TG_ERR_INVALID_ARGUMENT, "field_type must be TG_FIELD_F32 or TG_FIELD_F64");
-    cudaStream_t s = (cudaStream_t)stream;
-    m->last_stream = s;
-    if (!m->rel[TG_REL_VV].ready) TRY(tg_extract(m, TG_VV, 0, stream));
-    const int64_t V = m->V;
-    const Rel &vv = m->rel[TG_REL_VV];
-    if (!m->cadj) {
-        TRY(reset_status(m, s));
-        TRY(dalloc(&m->cadj, vv.entries, s));
-        int32_t *vv_win;
-        TRY(dalloc(&vv_win, window_count(vv.entries, crit_window()) + 1, s));
-        launch_window_starts(vv.off, V, vv.entries, crit_window(), vv_win, s);
-        // VV rows longer than the adjacency masks were already rejected by
-        // tg_extract (star pass A flags them), so no status read-back here
-        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st, s);
-        cudaFreeAsync(vv_win, s);
-    }
-    Temps tmp(s);
-    const size_t esz = field_type == TG_FIELD_F64 ? 8 : 4;
-    const void *f = field;
-    if (!field_on_device) {
-        char *d;
-        TRY(tmp.alloc(&d, (int64_t)(V * esz)));
-        CK(cudaMemcpyAsync(d, field, V * esz, cudaMemcpyHostToDevice, s));
-        f = d;
-    }
-    uint32_t *out = classes_out;
-    if (!out_on_device) TRY(tmp.alloc(&out, 3 * V));
-    launch_crit_classify(vv.off, vv.ent, m->cadj, f, field_type, V, out, s);
-    CK(cudaGetLastError());
-    if (!out_on_device) {
-        CK(cudaMemcpyAsync(classes_out, out, (size_t)V * 12, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-    }
-    return TG_OK;
+    if (!m) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
+    return critical_points_rows(m, 0, m->V, field, field_type, field_on_device, classes_out,
+                                out_on_device, (cudaStream_t)stream);
 }
 
 tg_status tg_profile_kernel(const char *name)

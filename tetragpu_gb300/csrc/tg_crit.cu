@@ -103,12 +103,16 @@ __device__ __forceinline__ int uf_find(unsigned char *p, int stride, int x)
 template <typename F>
 __global__ void __launch_bounds__(kClassifyThreads)
 k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
-                const unsigned long long *__restrict__ adj, const F *__restrict__ field, int64_t V,
-                unsigned *__restrict__ classes3)
+                const unsigned long long *__restrict__ adj, const F *__restrict__ field_v0,
+                int64_t v0, int64_t nv, unsigned *__restrict__ classes3_v0)
 {
+    // rows [v0, v0 + nv); field and classes indexed from v0 (a vertex range
+    // holds every neighbour of its vertices when it is a whole mesh of a batch)
     __shared__ unsigned char parent_all[kMaxDeg * kClassifyThreads];
-    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
+    const int64_t v = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= v0 + nv) return;
+    const F *field = field_v0 - v0;
+    unsigned *classes3 = classes3_v0 - 3 * v0;
     unsigned char *parent = parent_all + threadIdx.x;  // parent[k * stride]
     const int stride = kClassifyThreads;
     const int64_t b = vv_off[v];
@@ -167,19 +171,19 @@ void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
-                          const void *field, int field_type, int64_t V, uint32_t *classes3,
-                          cudaStream_t s)
+                          const void *field, int field_type, int64_t v0, int64_t nv,
+                          uint32_t *classes3, cudaStream_t s)
 {
-    if (V == 0) return;
-    const unsigned grid = (unsigned)((V + kClassifyThreads - 1) / kClassifyThreads);
+    if (nv == 0) return;
+    const unsigned grid = (unsigned)((nv + kClassifyThreads - 1) / kClassifyThreads);
     const auto *a = reinterpret_cast<const unsigned long long *>(adj);
     Launch L("k_crit_classify", s);
     if (field_type == 1)
         k_crit_classify<double><<<grid, kClassifyThreads, 0, s>>>(
-            vv_off, vv, a, (const double *)field, V, classes3);
+            vv_off, vv, a, (const double *)field, v0, nv, classes3);
     else
         k_crit_classify<float><<<grid, kClassifyThreads, 0, s>>>(
-            vv_off, vv, a, (const float *)field, V, classes3);
+            vv_off, vv, a, (const float *)field, v0, nv, classes3);
 }
 
 }  // namespace tg

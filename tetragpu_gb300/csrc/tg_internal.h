@@ -168,9 +168,10 @@ void launch_tt_vertex_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, co
 int crit_window();
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
                      int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s);
+// classify rows [v0, v0 + nv): field and classes3 hold nv values / rows from v0
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
-                          const void *field, int field_type, int64_t V, uint32_t *classes3,
-                          cudaStream_t s);
+                          const void *field, int field_type, int64_t v0, int64_t nv,
+                          uint32_t *classes3, cudaStream_t s);
 
 // the message tg_last_error_string returns on this thread
 void set_last_error(const char *msg);
@@ -179,6 +180,12 @@ void set_last_error(const char *msg);
 // followed by n + 1 first face ids (device, read by mesh_segment_ids).
 tg_status mesh_set_segments(tg_mesh *m, const int64_t *seg_c_host, int64_t n, cudaStream_t s);
 const int64_t *mesh_segment_ids(const tg_mesh *m);
+// tg_critical_points restricted to the vertices [v0, v0 + nv), which must
+// hold every neighbour of their vertices (a whole mesh of a batch): field
+// holds their nv values, classes_out their nv rows
+tg_status critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const void *field,
+                               int field_type, int field_on_device, uint32_t *classes_out,
+                               int out_on_device, cudaStream_t s);
 
 // launch accounting and optional CUDA-event timing of one named kernel
 void count_launch(int n = 1);
