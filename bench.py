@@ -46,8 +46,8 @@ WORKLOAD = "kuhn64_coned20_irregular"
 # --workload: the irregular single mesh (the headline), the 128^3 large mesh,
 # or the uneven 512-mesh batch (batched path against the per-mesh loop)
 WORKLOADS = {"irregular": "kuhn64_coned20_irregular", "large": "kuhn128_permuted_large",
-             "batch": "batch512_uneven_2k_400k"}
-DEFAULT_STEPS = {"irregular": 300, "large": 60, "batch": 5}
+             "batch": "batch512_uneven_2k_400k", "serve": "serve_poisson_70new_30field"}
+DEFAULT_STEPS = {"irregular": 300, "large": 60, "batch": 5, "serve": 1}
 
 
 def load_workload(key: str):
@@ -390,6 +390,127 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
         print(json.dumps(line), flush=True)
 
 
+def serve_requests(n_req: int, n_pool: int, seed: int):
+    """The request mix: a pool of seeded meshes (Kuhn grids, ids permuted, tet
+    counts lognormal with median 50k and sigma 1, capped at 4M) with four
+    Gaussian-mixture fields each; 70% of requests are new meshes drawn from the
+    pool, 30% new fields on a mesh an earlier request created."""
+    from tetragpu_gb300 import meshgen
+    rng = np.random.default_rng(seed)
+    pool = []
+    for i in range(n_pool):
+        target = float(min(4e6, np.exp(rng.normal(np.log(5e4), 1.0))))
+        dims = meshgen._dims_for(max(target, 6.0), rng)
+        m = meshgen.kuhn_mesh(dims, 0.0, seed=seed * 1000 + i)
+        m.fields = [meshgen.gaussian_mixture_field(m.coords, n_gauss=8, seed=seed * 1000 + i * 7 + k,
+                                                   noise=1e-3) for k in range(4)]
+        pool.append(m)
+    reqs = []   # ("mesh", pool index, field index) or ("field", earlier request, field index)
+    for r in range(n_req):
+        meshes_so_far = [k for k, q in enumerate(reqs) if q[0] == "mesh"]
+        if meshes_so_far and rng.random() < 0.3:
+            reqs.append(("field", int(rng.choice(meshes_so_far)), int(rng.integers(0, 4))))
+        else:
+            reqs.append(("mesh", int(rng.integers(0, n_pool)), int(rng.integers(0, 4))))
+    return pool, reqs
+
+
+def main_serve(args, torch, tg, rank):
+    """Serving: Poisson arrivals at swept rates into tg_server (continuous
+    batching, 150 GB budget), against the plain per-request path (each request
+    alone through tg_mesh_*, resident meshes kept under the same budget)."""
+    n_req = args.serve_requests
+    pool, reqs = serve_requests(n_req, 64, 2468)
+    tets = [pool[q[1]].n_cells if q[0] == "mesh" else pool[reqs[q[1]][1]].n_cells for q in reqs]
+    total_tets = int(sum(tets))
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    results = {}
+    for rate in rates:
+        rng = np.random.default_rng(int(rate))
+        gaps = rng.exponential(1.0 / rate, size=n_req)
+        with tg.Server(n_slots=4, hbm_budget_bytes=150 * 10**9) as srv:
+            rid, mid = [None] * n_req, [None] * n_req
+            t0 = time.perf_counter()
+            t_next = t0
+            for k, q in enumerate(reqs):
+                t_next += gaps[k]
+                while time.perf_counter() < t_next:
+                    pass
+                if q[0] == "mesh":
+                    m = pool[q[1]]
+                    rid[k], mid[k] = srv.submit_mesh(m.tv, m.n_verts, m.fields[q[2]])
+                else:
+                    m = pool[reqs[q[1]][1]]
+                    rid[k] = srv.submit_field(mid[q[1]], m.fields[q[2]])
+            lat = []
+            for k in range(n_req):
+                lat.append(srv.wait(rid[k])[1])
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        results[str(int(rate))] = {
+            "offered_req_per_s": rate, "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "mtets_per_s": round(total_tets / wall / 1e6, 3), "wall_s": round(wall, 3),
+            "batches": st["batches"], "meshes_built": st["meshes_built"],
+            "evictions": st["evictions"], "peak_gb": round(st["peak_bytes"] / 1e9, 2)}
+
+    # plain per-request path: one request at a time, back to back
+    budget = 150 * 10**9
+    resident, used, order = {}, 0, []
+    lat = []
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    t0 = time.perf_counter()
+    for k, q in enumerate(reqs):
+        t1 = time.perf_counter()
+        if q[0] == "mesh":
+            m = pool[q[1]]
+            g = tg.Mesh(m.tv, m.n_verts, stream=s)
+            g.extract(tg.ALL_RELATIONS, stream=s)
+            g.critical_points(m.fields[q[2]], stream=s)
+            b = g.device_bytes()
+            while order and used + b > budget:
+                old = order.pop(0)
+                used -= resident[old][1]
+                resident[old][0].close()
+                resident[old] = None
+            resident[k] = (g, b)
+            order.append(k)
+            used += b
+        else:
+            m = pool[reqs[q[1]][1]]
+            if resident.get(q[1]) is None:  # evicted: rebuild
+                g = tg.Mesh(m.tv, m.n_verts, stream=s)
+                g.extract(tg.ALL_RELATIONS, stream=s)
+                resident[q[1]] = (g, g.device_bytes())
+                order.append(q[1])
+                used += resident[q[1]][1]
+            resident[q[1]][0].critical_points(m.fields[q[2]], stream=s)
+        lat.append((time.perf_counter() - t1) * 1e3)
+    plain_wall = time.perf_counter() - t0
+    for v in resident.values():
+        if v is not None:
+            v[0].close()
+    plain = {"p50_ms": round(float(np.percentile(lat, 50)), 3),
+             "p99_ms": round(float(np.percentile(lat, 99)), 3),
+             "mtets_per_s": round(total_tets / plain_wall / 1e6, 3),
+             "wall_s": round(plain_wall, 3)}
+    if rank == 0:
+        top = results[str(int(rates[-1]))]
+        line = {
+            "metric": METRIC, "value": top["mtets_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": 1, "warmup": 0, "ms_per_step": round(top["wall_s"] * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOADS["serve"], "requests": n_req, "mesh_pool": len(pool),
+                       "tets_requested": total_tets, "budget_gb": 150, "slots": 4,
+                       "timing": "wall clock, submission to completion per request"},
+            "serving": results, "plain_per_request": plain,
+            "p99_ms": top["p99_ms"], "p50_ms": top["p50_ms"],
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -398,12 +519,15 @@ def main():
     ap.add_argument("--impl", default="tetragpu", choices=["tetragpu", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--workload", default="irregular", choices=sorted(WORKLOADS))
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-rates", default="500,2000,8000,32000",
+                    help="offered request rates (per second) for --workload serve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20 if args.impl == "reference" else DEFAULT_STEPS[args.workload]
     if args.impl == "reference":
-        if args.workload == "batch":
+        if args.workload in ("batch", "serve"):
             args.workload = "irregular"
         run_reference(args)
         return
@@ -422,6 +546,11 @@ def main():
         _build.build()
     tg.load()
 
+    if args.workload == "serve":
+        main_serve(args, torch, tg, rank)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     if args.workload == "batch":
         main_batch(args, torch, dist, tg, rank, local_rank, world)
         if world > 1:
