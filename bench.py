@@ -13,7 +13,10 @@ vertices), vertex ids permuted, float32 field = 32 Gaussians + N(0, 1e-3).
          (a 512 MB write) before every step, outside the timed window.
   e2e    the same steps through the C ABI with HOST buffers: pinned TV and
          field copied in, and every relation plus the classes copied back to
-         pinned host memory, all inside the timed window.
+         pinned host memory (tg_copy_relation_async), all inside the timed
+         window.  Steps alternate between two streams and two sets of host
+         buffers, so a step's copies back overlap the next step's extraction
+         (the host link, not the kernels, bounds this number).
 
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
 (the path does not shard within a mesh); value = tets of all ranks / max time.
@@ -619,41 +622,75 @@ def main():
     value = world * args.steps * T / t_max / 1e6
 
     # ---- e2e: host buffers through the C ABI ----
+    # Each step: pinned TV and field in, every relation and the classes out to
+    # pinned host memory.  Steps alternate between two streams and two sets
+    # of host buffers, so one step's copies back (host-link bound) overlap the
+    # next step's extraction, the way a caller processing many meshes would
+    # run; the timed region covers every copy of every step.
     pin_tv = torch.from_numpy(mesh.tv).pin_memory()
     pin_field = torch.from_numpy(mesh.field).pin_memory()
     names = tg.RELATIONS[1:]
     fixed_rows = {"TE": (Tc, 6), "EV": (E, 2), "TF": (Tc, 4), "FV": (F, 3), "FE": (F, 3),
                   "FT": (F, 2)}
     csr_rows = {"ET": E, "EF": E, "VT": Vc, "TT": Tc, "FF": F, "EE": E, "VV": Vc}
-    h_ent = {n: torch.empty(r * w, dtype=torch.int32).pin_memory() for n, (r, w) in fixed_rows.items()}
-    h_ent.update({n: torch.empty(totals[n], dtype=torch.int32).pin_memory() for n in csr_rows})
-    h_off = {n: torch.empty(r + 1, dtype=torch.int64).pin_memory() for n, r in csr_rows.items()}
-    h_cls = np.empty((V, 3), dtype=np.uint32)
+    bufs = []
+    for _ in range(2):
+        h_ent = {n: torch.empty(max(r * w, 1), dtype=torch.int32).pin_memory()
+                 for n, (r, w) in fixed_rows.items()}
+        h_ent.update({n: torch.empty(max(totals[n], 1), dtype=torch.int32).pin_memory()
+                      for n in csr_rows})
+        h_off = {n: torch.empty(r + 1, dtype=torch.int64).pin_memory() for n, r in csr_rows.items()}
+        h_cls = torch.empty(3 * V, dtype=torch.int32).pin_memory()
+        bufs.append((h_ent, h_off, h_cls))
     h2d = pin_tv.numel() * 4 + pin_field.numel() * 4
-    d2h = sum(x.numel() * 4 for x in h_ent.values()) + sum(x.numel() * 8 for x in h_off.values()) \
-        + h_cls.nbytes
+    d2h = sum(r * w * 4 for r, w in fixed_rows.values()) + sum(totals[n] * 4 for n in csr_rows) \
+        + sum((r + 1) * 8 for r in csr_rows.values()) + V * 12
     lib = tg.load()
+    dev = f"cuda:{local_rank}"
+    e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    d_cls2 = [torch.empty(3 * V, dtype=torch.int32, device=dev) for _ in range(2)]
+    d_tv2 = [torch.empty_like(d_tv) for _ in range(2)]
+    d_f2 = [torch.empty_like(d_field) for _ in range(2)]
 
-    def e2e_step():
-        with tg.Mesh(pin_tv.numpy(), V, stream=s) as g:
-            g.extract(tg.ALL_RELATIONS, stream=s)
-            tg._lib.check(lib.tg_critical_points(g._h, pin_field.data_ptr(), tg.FIELD_F32, 0,
-                                                 h_cls.ctypes.data, 0, s))
+    def upload(k):
+        # a step's inputs go up before the previous step's results come down:
+        # the copies share one queue, so an upload behind them would wait
+        with torch.cuda.stream(e_streams[k % 2]):
+            d_tv2[k % 2].copy_(pin_tv, non_blocking=True)
+            d_f2[k % 2].copy_(pin_field, non_blocking=True)
+
+    def e2e_run(n_steps):
+        live = None
+        upload(0)
+        for k in range(n_steps):
+            es = e_streams[k % 2].cuda_stream
+            h_ent, h_off, h_cls = bufs[k % 2]
+            g = tg.Mesh(d_tv2[k % 2].data_ptr(), V, n_cells=T, on_device=True, stream=es)
+            g.extract(tg.ALL_RELATIONS, stream=es)
+            tg._lib.check(lib.tg_critical_points(g._h, d_f2[k % 2].data_ptr(), tg.FIELD_F32, 1,
+                                                 d_cls2[k % 2].data_ptr(), 1, es))
+            if k + 1 < n_steps:
+                upload(k + 1)
             for n in names:
-                tg._lib.check(lib.tg_copy_relation(
+                tg._lib.check(lib.tg_copy_relation_async(
                     g._h, tg.REL[n], h_off[n].data_ptr() if n in h_off else None,
-                    h_ent[n].data_ptr() if h_ent[n].numel() else None, s))
+                    h_ent[n].data_ptr(), es))
+            with torch.cuda.stream(e_streams[k % 2]):
+                h_cls.copy_(d_cls2[k % 2], non_blocking=True)
+            if live is not None:
+                live.close()        # waits for the previous step's copies
+            live = g
+        if live is not None:
+            live.close()
+        torch.cuda.synchronize()
 
     e2e_value = None
     if args.e2e_steps > 0:
-        e2e_step()
-        torch.cuda.synchronize()
+        e2e_run(2)
         if world > 1:
             dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            e2e_step()
-        torch.cuda.synchronize()
+        e2e_run(args.e2e_steps)
         e2e_s = time.perf_counter() - t0
         if world > 1:
             t = torch.tensor([e2e_s], device=f"cuda:{local_rank}", dtype=torch.float64)

@@ -134,6 +134,12 @@ tg_status tg_get_relation(const tg_mesh *mesh, int relation, const int64_t **off
  * to skip them).  Synchronous with respect to the host. */
 tg_status tg_copy_relation(const tg_mesh *mesh, int relation, int64_t *offsets_host,
                            int32_t *entries_host, void *stream);
+/* The same copies issued on `stream` without waiting for them: a caller that
+ * processes many meshes overlaps one mesh's copies with the next one's
+ * extraction (pinned host buffers; destroy the mesh, which waits for its last
+ * stream, or synchronise the stream before reading the buffers). */
+tg_status tg_copy_relation_async(tg_mesh *mesh, int relation, int64_t *offsets_host,
+                                 int32_t *entries_host, void *stream);
 
 /* A relation's entries widened to int64 (the reference's vtkIdType) and its
  * int64 offsets (CSR only; may be NULL), into caller memory on the device

@@ -62,6 +62,7 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_mesh_counts": (C.c_int, [vp, P(i64), P(i64), P(i64), P(i64)]),
         "tg_get_relation": (C.c_int, [vp, C.c_int, P(vp), P(vp), P(i64), P(i64), P(i32)]),
         "tg_copy_relation": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "tg_copy_relation_async": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "tg_get_tv": (C.c_int, [vp, P(vp)]),
         "tg_export_relation_i64": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp]),
         "tg_export_rows_padded": (C.c_int, [vp, C.c_int, i32, vp, vp, vp]),

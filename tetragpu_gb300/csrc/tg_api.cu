@@ -126,9 +126,12 @@ void setup_pool(int dev)
     g_pool_ready[dev] = true;
 }
 
-// Pinned host slots for the status word and the sizes read back at the
-// synchronisation points: pinned allocation is slow, so slots come from a
-// process-wide pool of 4 KiB chunks and are recycled.
+// Pinned, device-mapped host slots for the status word and the sizes read
+// back at the synchronisation points: a kernel stores them there directly,
+// so a read-back never queues behind large copies in flight on the copy
+// engines (a caller draining an earlier mesh's relations).  Pinned
+// allocation is slow, so slots come from a process-wide pool of 4 KiB
+// chunks and are recycled.
 struct PinnedPool {
     std::mutex mu;
     std::vector<void *> free_slots;
@@ -137,7 +140,8 @@ struct PinnedPool {
         std::lock_guard<std::mutex> lk(mu);
         if (free_slots.empty()) {
             char *chunk = nullptr;
-            if (cudaMallocHost((void **)&chunk, 4096) != cudaSuccess) return nullptr;
+            if (cudaHostAlloc((void **)&chunk, 4096, cudaHostAllocMapped) != cudaSuccess)
+                return nullptr;
             for (int i = 0; i < 16; i++) free_slots.push_back(chunk + 256 * i);
         }
         void *p = free_slots.back();
@@ -265,14 +269,18 @@ tg_status reset_status(tg_mesh *m, cudaStream_t s)
 // else int32) into m->sz_host, synchronously.
 tg_status sync_read(tg_mesh *m, cudaStream_t s, int n, const void *const *src, const bool *wide)
 {
-    CK(cudaMemcpyAsync(m->st_host, m->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    PublishArgs a{};
+    a.st = m->st;
+    a.n = n;
     for (int i = 0; i < n; i++) {
-        m->sz_host[i] = 0;
-        CK(cudaMemcpyAsync(&m->sz_host[i], src[i], wide[i] ? 8 : 4, cudaMemcpyDeviceToHost, s));
+        a.src[i] = src[i];
+        a.wide[i] = wide[i] ? 1 : 0;
     }
+    CK(cudaHostGetDevicePointer((void **)&a.h_st, m->st_host, 0));
+    CK(cudaHostGetDevicePointer((void **)&a.h_sz, m->sz_host, 0));
+    launch_publish(a, s);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
-    for (int i = 0; i < n; i++)
-        if (!wide[i]) m->sz_host[i] = (int64_t)(int32_t)m->sz_host[i];
     return TG_OK;
 }
 
@@ -758,6 +766,21 @@ tg_status tg_copy_relation(const tg_mesh *m, int r, int64_t *off_host, int32_t *
     if (ent_host && x.entries)
         CK(cudaMemcpyAsync(ent_host, x.ent, (size_t)x.entries * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+
+tg_status tg_copy_relation_async(tg_mesh *m, int r, int64_t *off_host, int32_t *ent_host,
+                                 void *stream)
+{
+    if (!m || r < 1 || r > 13) return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh or relation index");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    cudaStream_t s = (cudaStream_t)stream;
+    m->last_stream = s;
+    if (off_host && x.off)
+        CK(cudaMemcpyAsync(off_host, x.off, (size_t)(x.rows + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (ent_host && x.entries)
+        CK(cudaMemcpyAsync(ent_host, x.ent, (size_t)x.entries * 4, cudaMemcpyDeviceToHost, s));
     return TG_OK;
 }
 

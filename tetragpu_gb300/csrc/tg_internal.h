@@ -61,6 +61,17 @@ struct Sizes {
 };
 
 void launch_reset_status(DevStatus *st, cudaStream_t s);
+// Status word and up to 8 sizes (int64, or int32 sign-extended) stored by a
+// kernel into device-mapped pinned host memory (no copy engine involved)
+struct PublishArgs {
+    const DevStatus *st;
+    const void *src[8];
+    int wide[8];
+    int n;
+    DevStatus *h_st;
+    int64_t *h_sz;
+};
+void launch_publish(const PublishArgs &a, cudaStream_t s);
 void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s);
 void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
                      int64_t *out, uint32_t *counts, cudaStream_t s);

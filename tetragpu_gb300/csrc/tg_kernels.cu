@@ -441,6 +441,21 @@ void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int w
                                                             reinterpret_cast<long long *>(out), counts);
 }
 
+__global__ void k_publish(PublishArgs a)
+{
+    if (threadIdx.x != 0) return;
+    *a.h_st = *a.st;
+    for (int i = 0; i < a.n; i++)
+        a.h_sz[i] = a.wide[i] ? *(const int64_t *)a.src[i] : (int64_t) * (const int32_t *)a.src[i];
+    __threadfence_system();
+}
+
+void launch_publish(const PublishArgs &a, cudaStream_t s)
+{
+    Launch L("k_publish", s);
+    k_publish<<<1, 32, 0, s>>>(a);
+}
+
 void launch_reset_status(DevStatus *st, cudaStream_t s)
 {
     Launch L("k_reset_status", s);
