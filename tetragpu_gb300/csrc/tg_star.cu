@@ -211,11 +211,16 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
         S.meta[e] = m | (sv << 20);
         const int ewarp = e - (threadIdx.x & 31);  // entry of lane 0 of this warp
         const int shift = ewarp - rs;               // lane l sits at row position l + shift
+        // the lanes holding this row's entries are contiguous: match on the
+        // neighbour alone and keep those lanes
+        const int lo = max(-shift, 0), hi = min(-shift + m_D(m), 32);
+        const unsigned rowmask = (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int t = k + (k >= sv);
-            const unsigned long long key = hk(rs, get4(w, t));
-            const unsigned grp = __match_any_sync(amask, key);
+            const int u = get4(w, t);
+            const unsigned long long key = hk(rs, u);
+            const unsigned grp = __match_any_sync(amask, u) & rowmask;
             const int leader = __ffs(grp) - 1;
             int h = 0;
             if ((int)(threadIdx.x & 31) == leader) {
