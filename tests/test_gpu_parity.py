@@ -124,3 +124,63 @@ def test_irregular_full(gpu_lib, oracle):
             else:
                 assert np.array_equal(got, want), n
         assert np.array_equal(g.critical_points(m.field), ref_cp)
+
+
+def _fan(n_tets):
+    # n_tets tets sharing only vertex 0 (faces all distinct: a valid mesh)
+    tv = np.array([[0, 3 * i + 1, 3 * i + 2, 3 * i + 3] for i in range(n_tets)], np.int32)
+    return tv, 3 * n_tets + 1
+
+
+@pytest.mark.parametrize("n_tets", [70, 30])
+def test_beyond_star_limits_is_unsupported(gpu_lib, oracle, n_tets):
+    # 70 cells around a vertex exceed the 64-cell star; 30 give 90 neighbours,
+    # beyond the 64 a link mask holds.  Both are refused with a status, and
+    # the device stays usable.
+    tv, nv = _fan(n_tets)
+    with gpu_lib.Mesh(tv, nv) as g:
+        with pytest.raises(gpu_lib.TetraGPUError) as ei:
+            g.extract(gpu_lib.ALL_RELATIONS)
+        assert ei.value.code == 5
+    _check_mesh(gpu_lib, oracle, meshgen.kuhn_mesh(2, 0.5, seed=3))
+
+
+def test_large_mesh_properties(gpu_lib):
+    """The 128^3 workload (12.6M tets): counts, size identities, sorted rows,
+    symmetric VV and critical-point codes, checked without the oracle."""
+    m = meshgen.workload_large()
+    T, V = m.n_cells, m.n_verts
+    with gpu_lib.Mesh(m.tv, V) as g:
+        g.extract(gpu_lib.ALL_RELATIONS)
+        v, e, f, t = g.counts()
+        assert (v, e, f, t) == (2146689, 14827904, 25264128, 12582912)
+        assert v - e + f - t == 1                      # a solid cube
+        et_off, et = g.relation("ET")
+        ef_off, _ = g.relation("EF")
+        assert et_off[-1] == 6 * T and ef_off[-1] == 3 * f
+        vt_off, vt = g.relation("VT")
+        assert vt_off[-1] == 4 * T
+        vv_off, vv = g.relation("VV")
+        assert vv_off[-1] == 2 * e
+        # rows ascending
+        for off, ent in ((vv_off, vv), (vt_off, vt), (et_off, et)):
+            d = np.diff(ent.astype(np.int64))
+            starts = np.zeros(ent.size, bool)
+            starts[off[1:-1][off[1:-1] < ent.size]] = True
+            assert (d[~starts[1:]] > 0).all()
+        # VV symmetric: (v, u) present iff (u, v)
+        rows = np.repeat(np.arange(V, dtype=np.int64), np.diff(vv_off))
+        fwd = rows * V + vv
+        bwd = vv.astype(np.int64) * V + rows
+        assert np.array_equal(np.sort(fwd), np.sort(bwd))
+        te = g.relation("TE")
+        assert te.min() == 0 and te.max() == e - 1
+        ft = g.relation("FT")
+        n_bnd = int((ft[:, 1] < 0).sum())
+        assert n_bnd == 6 * 2 * 128 * 128              # two triangles per boundary square
+        tt_off, _ = g.relation("TT")
+        assert tt_off[-1] == 4 * T - n_bnd
+        cp = g.critical_points(m.field)
+        assert set(np.unique(cp[:, 2])) <= {1, 2, 3, 4}
+        regular = cp[:, 2] == 3
+        assert ((cp[regular, 0] == 1) & (cp[regular, 1] == 1)).all()
