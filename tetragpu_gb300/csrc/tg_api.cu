@@ -639,8 +639,10 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     }
     Temps tmp(s);
     int32_t *deg_t;
+    int4 *occ;
     TRY(tmp.alloc(&deg_t, V, true));
-    launch_canon(src, T, V, m->tvs, deg_t, m->st, s);
+    TRY(tmp.alloc(&occ, T));
+    launch_canon(src, T, V, m->tvs, deg_t, occ, m->st, s);
     int64_t *vt_off;
     int32_t *vt;
     TRY(dalloc(&vt_off, V + 1, s));
@@ -648,9 +650,8 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(std::max(V, (4 * T + 31) / 32)) + 256));
     ScanJob job{deg_t, vt_off, V, SCAN_COUNT_I32, 0};
     scan_batch(&job, 1, scratch, s);
-    CK(cudaMemsetAsync(deg_t, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
     TRY(dalloc(&vt, 4 * T, s));
-    launch_vt_fill(m->tvs, T, vt_off, deg_t, vt, s);
+    launch_vt_fill(m->tvs, T, vt_off, occ, vt, s);
     TRY(dalloc(&m->vt_win, window_count(4 * T, star_window()) + 1, s));
     launch_window_starts(vt_off, V, 4 * T, star_window(), m->vt_win, s);
     // VT row sort, which also marks each vertex's star-order key; then the

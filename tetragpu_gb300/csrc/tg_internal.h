@@ -75,9 +75,11 @@ void launch_publish(const PublishArgs &a, cudaStream_t s);
 void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s);
 void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
                      int64_t *out, uint32_t *counts, cudaStream_t s);
+// sort each TV row, validate ids, count cells per vertex; occ[c] = the
+// cell's place in each of its vertices' (unsorted) VT rows
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
-                  DevStatus *st, cudaStream_t s);
-void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, int32_t *cursor,
+                  int4 *occ, DevStatus *st, cudaStream_t s);
+void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, const int4 *occ,
                     int32_t *vt, cudaStream_t s);
 void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStream_t s);
 // Windows of win_size entries over a CSR: win[w] = first row starting at or

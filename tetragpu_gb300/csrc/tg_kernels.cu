@@ -83,7 +83,8 @@ __device__ __forceinline__ int lower_bound_sm(const int *a, int n, int key)
 // k_canon
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
-k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, DevStatus *st, int aligned)
+k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, int4 *occ, DevStatus *st,
+        int aligned)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
@@ -116,10 +117,10 @@ k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, DevStatus *s
         return;
     }
     tvs[c] = make_int4(a, b, d, e);
-    atomicAdd(deg_t + a, 1);
-    atomicAdd(deg_t + b, 1);
-    atomicAdd(deg_t + d, 1);
-    atomicAdd(deg_t + e, 1);
+    // the count so far is the cell's place in each vertex's VT row (rows are
+    // sorted afterwards)
+    occ[c] = make_int4(atomicAdd(deg_t + a, 1), atomicAdd(deg_t + b, 1), atomicAdd(deg_t + d, 1),
+                       atomicAdd(deg_t + e, 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -127,16 +128,17 @@ k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, DevStatus *s
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 k_vt_fill(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__ vt_off,
-          int *__restrict__ cursor, int *__restrict__ vt)
+          const int4 *__restrict__ occ, int *__restrict__ vt)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     const int4 w = tvs[c];
     if (w.x < 0) return;  // rejected by k_canon
-    vt[vt_off[w.x] + atomicAdd(cursor + w.x, 1)] = (int)c;
-    vt[vt_off[w.y] + atomicAdd(cursor + w.y, 1)] = (int)c;
-    vt[vt_off[w.z] + atomicAdd(cursor + w.z, 1)] = (int)c;
-    vt[vt_off[w.w] + atomicAdd(cursor + w.w, 1)] = (int)c;
+    const int4 o = occ[c];
+    vt[vt_off[w.x] + o.x] = (int)c;
+    vt[vt_off[w.y] + o.y] = (int)c;
+    vt[vt_off[w.z] + o.z] = (int)c;
+    vt[vt_off[w.w] + o.w] = (int)c;
 }
 
 __global__ void __launch_bounds__(256)
@@ -463,23 +465,23 @@ void launch_reset_status(DevStatus *st, cudaStream_t s)
 }
 
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
-                  DevStatus *st, cudaStream_t s)
+                  int4 *occ, DevStatus *st, cudaStream_t s)
 {
     if (T == 0) return;
     const int aligned = ((uintptr_t)tv_in & 15) == 0;
     {
         Launch L("k_canon", s);
-        k_canon<<<blocks_for(T, 256), 256, 0, s>>>(tv_in, T, (int)V, tvs, deg_t, st, aligned);
+        k_canon<<<blocks_for(T, 256), 256, 0, s>>>(tv_in, T, (int)V, tvs, deg_t, occ, st, aligned);
     }
 }
 
-void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, int32_t *cursor, int32_t *vt,
+void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, const int4 *occ, int32_t *vt,
                     cudaStream_t s)
 {
     if (T == 0) return;
     {
         Launch L("k_vt_fill", s);
-        k_vt_fill<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, vt_off, cursor, vt);
+        k_vt_fill<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, vt_off, occ, vt);
     }
 }
 
