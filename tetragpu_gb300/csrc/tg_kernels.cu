@@ -312,6 +312,62 @@ __device__ __forceinline__ void ee_merge_one(const int *__restrict__ eid, int64_
     }
 }
 
+// Rows of at most 16 entries each (the common case: 14 neighbours inside a
+// Kuhn grid) go four edges at a time, eight lanes to an edge, four
+// registers to a lane (position gl + 8 r): the same bitonic merge over 32
+// positions with two register stages and three shuffle stages.
+__device__ __forceinline__ void ee_merge_group(const int *__restrict__ eid, int64_t ra, int na,
+                                               int64_t rb, int nb, int ei, int *__restrict__ out,
+                                               int gl, int g)
+{
+    int x[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int p = gl + 8 * r;
+        if (r < 2) {
+            x[r] = p < na ? __ldg(eid + ra + p) : INT_MAX;
+        } else {
+            const int j = 31 - p;
+            x[r] = j < nb ? __ldg(eid + rb + j) : INT_MAX;
+        }
+    }
+    // stride 16: registers r, r + 2; stride 8: r, r + 1
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int lo = min(x[r], x[r + 2]), hi = max(x[r], x[r + 2]);
+        x[r] = lo;
+        x[r + 2] = hi;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r += 2) {
+        const int lo = min(x[r], x[r + 1]), hi = max(x[r], x[r + 1]);
+        x[r] = lo;
+        x[r + 1] = hi;
+    }
+    // strides 4, 2, 1: lanes of the group
+#pragma unroll
+    for (int sl = 4; sl >= 1; sl >>= 1) {
+        const bool upper = gl & sl;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int y = __shfl_xor_sync(kFull, x[r], sl);
+            x[r] = upper ? max(x[r], y) : min(x[r], y);
+        }
+    }
+    int pe = 32;
+#pragma unroll
+    for (int r = 3; r >= 0; r--) {
+        const unsigned m = (__ballot_sync(kFull, x[r] == ei) >> (8 * g)) & 0xffu;
+        if (m) pe = 8 * r + __ffs(m) - 1;
+    }
+    const int n = na + nb;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int p = gl + 8 * r;
+        if (p < n && x[r] != ei) out[p - (p > pe ? 2 : 0)] = x[r];
+    }
+}
+
 __global__ void __launch_bounds__(kEeWarps * 32)
 k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_off,
           const int *__restrict__ eid, const int64_t *__restrict__ ee_off, int *__restrict__ ee)
@@ -330,15 +386,28 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
         my_nb = (int)(__ldg(vv_off + ab.y + 1) - my_rb);
         my_out = __ldg(ee_off + e0 + lane);
     }
-    for (int j = 0; j < cnt; j++) {
+    const unsigned small = __ballot_sync(kFull, lane < cnt && max(my_na, my_nb) <= 16);
+    const unsigned big = __ballot_sync(kFull, lane < cnt) & ~small;
+    // small edges, four per round (group g takes the (4 k + g)-th one)
+    const int g = lane >> 3, gl = lane & 7;
+    const int n_small = __popc(small);
+    for (int k = 0; k < n_small; k += 4) {
+        const int which = k + g;
+        const int src = which < n_small ? (int)__fns(small, 0, which + 1) : 0;
+        const int64_t ra = __shfl_sync(kFull, my_ra, src), rb = __shfl_sync(kFull, my_rb, src);
+        int na = __shfl_sync(kFull, my_na, src), nb = __shfl_sync(kFull, my_nb, src);
+        const int64_t o = __shfl_sync(kFull, my_out, src);
+        if (which >= n_small) na = nb = 0;  // an idle group: nothing to write
+        ee_merge_group(eid, ra, na, rb, nb, (int)(e0 + src), ee + o, gl, g);
+    }
+    // longer rows one edge at a time over the whole warp
+    for (unsigned rest = big; rest; rest &= rest - 1) {
+        const int j = __ffs(rest) - 1;
         const int64_t ra = __shfl_sync(kFull, my_ra, j), rb = __shfl_sync(kFull, my_rb, j);
         const int na = __shfl_sync(kFull, my_na, j), nb = __shfl_sync(kFull, my_nb, j);
         int *out = ee + __shfl_sync(kFull, my_out, j);
         const int ei = (int)(e0 + j);
-        const int mx = max(na, nb);
-        if (mx <= 16)
-            ee_merge_one<1>(eid, ra, na, rb, nb, ei, out, lane);
-        else if (mx <= 32)
+        if (max(na, nb) <= 32)
             ee_merge_one<2>(eid, ra, na, rb, nb, ei, out, lane);
         else
             ee_merge_one<4>(eid, ra, na, rb, nb, ei, out, lane);
