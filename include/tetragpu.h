@@ -175,6 +175,16 @@ tg_status tg_critical_points(tg_mesh *mesh, const void *field, int field_type,
                              int field_on_device, uint32_t *classes_out,
                              int out_on_device, void *stream);
 
+/* The reference's class report (export_classes, src/alg/critPoints.cu:340-453)
+ * for classes in host memory (the tg_critical_points layout): the five
+ * "Total number of ..." lines with the reference's wording and numbers (its
+ * labels are swapped: "minima" counts code 2, the true maxima), preceded, if
+ * per_vertex_lines, by one "A <vertex> <code>" line per classified vertex
+ * (the form its verifier script parses).  path NULL writes to stdout.
+ * counts_out (may be NULL): vertices per code 0..4.  Host only. */
+tg_status tg_export_classes(const uint32_t *classes, int64_t n_verts, const char *path,
+                            int per_vertex_lines, int64_t *counts_out);
+
 /* Bytes of device memory the mesh currently holds. */
 int64_t tg_mesh_device_bytes(const tg_mesh *mesh);
 

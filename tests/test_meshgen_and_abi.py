@@ -73,3 +73,28 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
             _lib.load(str(tmp_path / "libtetragpu.so"))
         finally:
             _lib._lib = _lib._lib_backup
+
+
+def test_class_report_matches_the_reference_wording(tmp_path):
+    """tg_export_classes (host only): the reference's totals, with its swapped
+    labels, and the per-vertex lines its verifier reads."""
+    import tetragpu_gb300 as tg
+    from tetragpu_gb300 import _build
+    if not os.path.exists(_build.LIB):
+        pytest.skip("library not built")
+    # (lower-link components, upper-link components, code)
+    cls = np.array([[1, 0, 2],      # only lower neighbours: code 2, a true maximum
+                    [0, 1, 1],      # code 1, a true minimum
+                    [1, 1, 3],
+                    [2, 2, 4],
+                    [0, 0, 4],
+                    [0, 1, 3]],     # disagrees with its counts: reported, still counted
+                   dtype=np.uint32)
+    path = tmp_path / "classes.txt"
+    counts = tg.export_classes(cls, str(path), per_vertex_lines=True)
+    assert counts == [0, 1, 1, 2, 2]
+    lines = path.read_text().splitlines()
+    assert lines[:6] == ["A 0 2", "A 1 1", "A 2 3", "A 3 4", "A 4 4", "A 5 3"]
+    assert lines[6:] == ["Total number of minima:  1", "Total number of maxima:  1",
+                         "Total number of saddles: 2", "Total number of regular: 2",
+                         "Total number of voids:   0"]

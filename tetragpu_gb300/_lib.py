@@ -80,6 +80,7 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_batch_relation_size": (C.c_int, [vp, i64, C.c_int, P(i64), P(i64), P(i32)]),
         "tg_batch_copy_relation": (C.c_int, [vp, i64, C.c_int, vp, vp, vp]),
         "tg_batch_union": (vp, [vp]),
+        "tg_export_classes": (C.c_int, [vp, i64, C.c_char_p, C.c_int, P(i64)]),
         "tg_server_create": (C.c_int, [C.c_int, vp, P(vp)]),
         "tg_server_destroy": (C.c_int, [vp]),
         "tg_server_submit_mesh": (C.c_int, [vp, vp, i64, i64, vp, C.c_int, P(i64), P(i64)]),
@@ -431,6 +432,16 @@ class Server:
         st = _ServerStats()
         check(self._lib.tg_server_get_stats(self._h, C.byref(st)))
         return {n: getattr(st, n) for n, _ in _ServerStats._fields_}
+
+
+def export_classes(classes, path: str | None = None, per_vertex_lines: bool = False) -> list:
+    """The reference's class report (see tg_export_classes); returns the
+    vertex count per code 0..4."""
+    cls = np.ascontiguousarray(classes, dtype=np.uint32).reshape(-1, 3)
+    counts = (C.c_int64 * 5)()
+    check(load().tg_export_classes(cls.ctypes.data if cls.size else None, cls.shape[0],
+                                   path.encode() if path else None, int(per_vertex_lines), counts))
+    return list(counts)
 
 
 def kernel_launch_count() -> int:
