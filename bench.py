@@ -68,6 +68,13 @@ def env_rank():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def max_over_ranks(x: float, dist, torch, device) -> float:
+    """The slowest rank's time: replicas share nothing but this reduction."""
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -317,9 +324,7 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
         torch.cuda.synchronize()
         total = sum(a.elapsed_time(b) for a, b in ev) / 1e3
         if world > 1:
-            t = torch.tensor([total], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total = float(t.item())
+            total = max_over_ranks(total, dist, torch, dev)
         return total, tg.kernel_launch_count() - l0
 
     clocks = Clocks(local_rank)
@@ -615,9 +620,7 @@ def main():
     total_s = sum(ms) / 1e3
     t_max = total_s
     if world > 1:
-        t = torch.tensor([total_s], device=f"cuda:{local_rank}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+        t_max = max_over_ranks(total_s, dist, torch, f"cuda:{local_rank}")
         dist.barrier()
     value = world * args.steps * T / t_max / 1e6
 
@@ -693,9 +696,7 @@ def main():
         e2e_run(args.e2e_steps)
         e2e_s = time.perf_counter() - t0
         if world > 1:
-            t = torch.tensor([e2e_s], device=f"cuda:{local_rank}", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+            e2e_s = max_over_ranks(e2e_s, dist, torch, f"cuda:{local_rank}")
         e2e_value = round(world * args.e2e_steps * T / e2e_s / 1e6, 3)
 
     if rank == 0:
