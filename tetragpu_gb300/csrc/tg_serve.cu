@@ -2,8 +2,8 @@
 //
 // Requests are new meshes (each with a field) and new fields on resident
 // meshes.  n_slots worker threads, each with its own CUDA stream, take work
-// from one FIFO queue: a field request alone, or every new-mesh request at
-// the head of the queue that fits the batch size and the device-memory
+// from one queue: a field request at its head alone, or the new-mesh
+// requests near its head that fit the batch size and the device-memory
 // budget, merged into one batch (tg_batch_*, the disjoint union).  Requests
 // that arrive while the slots are busy therefore join the next batch, and the
 // slots' work overlaps on the device.  A finished batch stays resident
@@ -99,6 +99,9 @@ struct tg_server {
     // one stream per slot; they outlive the workers, because a resident
     // batch's frees are ordered on the stream it was last used on
     std::vector<cudaStream_t> streams;
+    // batches dropped under the lock and freed after it is released (a free
+    // waits for the batch's last stream, which may be busy with other work)
+    std::vector<tg_batch *> graveyard;
 };
 
 namespace {
@@ -131,7 +134,7 @@ void evict_idle(tg_server *S, int64_t need)
         for (auto &kv : S->meshes)
             if (kv.second->g == g) kv.second->g.reset();
         S->groups.erase(std::find(S->groups.begin(), S->groups.end(), g));
-        tg_batch_destroy(g->b);
+        S->graveyard.push_back(g->b);
         g->b = nullptr;
         S->used -= g->bytes;
         freed += g->bytes;
@@ -145,13 +148,31 @@ void drop_group_if_unused(tg_server *S, const std::shared_ptr<Group> &g)
     auto it = std::find(S->groups.begin(), S->groups.end(), g);
     if (it == S->groups.end()) return;
     S->groups.erase(it);
-    tg_batch_destroy(g->b);
+    S->graveyard.push_back(g->b);
     g->b = nullptr;
     S->used -= g->bytes;
 }
 
-// Take the next unit of work from the head of the queue.  Called with S->mu
-// held; false when the head must wait for memory.
+// Free the batches dropped under the lock.  Called without S->mu held.
+void bury(tg_server *S)
+{
+    std::vector<tg_batch *> dead;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        dead.swap(S->graveyard);
+    }
+    for (tg_batch *b : dead) tg_batch_destroy(b);
+}
+
+// Take the next unit of work.  A field request at the head of the queue goes
+// alone.  Otherwise the new-mesh requests among the first kScan queued (field
+// requests stay where they are) are gathered into one batch, in queue order,
+// while they fit the batch size and the memory budget.  A field request is
+// never passed by its own mesh's request (that request is ahead of it), so
+// moving new meshes forward keeps every field after its mesh.  Called with
+// S->mu held; false when the head must wait for memory.
+constexpr size_t kScan = 1024;
+
 bool take_work(tg_server *S, std::vector<std::shared_ptr<Req>> &work, int64_t &est)
 {
     auto &q = S->queue;
@@ -163,27 +184,35 @@ bool take_work(tg_server *S, std::vector<std::shared_ptr<Req>> &work, int64_t &e
     }
     const int64_t budget = S->cfg.hbm_budget_bytes;
     int64_t cells = 0;
-    size_t k = 0;
     est = 0;
     const int ftype = q.front()->ftype;
-    while (k < q.size() && q[k]->kind == kMesh && q[k]->ftype == ftype) {
+    std::vector<size_t> pick;
+    for (size_t k = 0; k < q.size() && k < kScan; k++) {
+        if (q[k]->kind != kMesh || q[k]->ftype != ftype) continue;
         const MeshRec &m = *q[k]->mesh;
-        if (k > 0 && cells + m.T > S->cfg.batch_cells) break;
+        if (!pick.empty() && cells + m.T > S->cfg.batch_cells) break;
         const int64_t e = estimate(m.T, m.V);
         if (S->used + est + e > budget) {
             evict_idle(S, S->used + est + e - budget);
             // nothing in flight will free memory: let a lone request run over
-            if (S->used + est + e > budget && !(k == 0 && S->in_flight == 0)) break;
+            if (S->used + est + e > budget && !(pick.empty() && S->in_flight == 0)) break;
         }
         est += e;
         cells += m.T;
-        k++;
+        pick.push_back(k);
     }
-    if (k == 0) return false;
-    for (size_t i = 0; i < k; i++) {
-        work.push_back(q.front());
-        q.pop_front();
+    if (pick.empty()) return false;
+    std::deque<std::shared_ptr<Req>> rest;
+    size_t next = 0;
+    for (size_t k = 0; k < q.size(); k++) {
+        if (next < pick.size() && pick[next] == k) {
+            work.push_back(q[k]);
+            next++;
+        } else {
+            rest.push_back(q[k]);
+        }
     }
+    q.swap(rest);
     S->used += est;
     note_used(S);
     return true;
@@ -447,10 +476,12 @@ void worker(tg_server *S, cudaStream_t s)
             }
             S->in_flight++;
         }
+        bury(S);
         if (work[0]->kind == kField)
             run_field(S, work[0], s);
         else
             run_meshes(S, work, est, s);
+        bury(S);
     }
 }
 
@@ -500,6 +531,7 @@ tg_status tg_server_destroy(tg_server *S)
     }
     S->cv_work.notify_all();
     for (auto &t : S->workers) t.join();
+    bury(S);
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(S->device);
@@ -620,6 +652,7 @@ tg_status tg_server_relation_size(tg_server *S, int64_t mesh_id, int relation, i
         }
         release_busy(S, g);
     }
+    bury(S);
     cudaSetDevice(cur);
     return st;
 }
@@ -645,6 +678,7 @@ tg_status tg_server_copy_relation(tg_server *S, int64_t mesh_id, int relation,
         }
         release_busy(S, g);
     }
+    bury(S);
     cudaSetDevice(cur);
     return st;
 }
@@ -652,15 +686,19 @@ tg_status tg_server_copy_relation(tg_server *S, int64_t mesh_id, int relation,
 tg_status tg_server_release_mesh(tg_server *S, int64_t mesh_id)
 {
     if (!S) return sfail(TG_ERR_INVALID_ARGUMENT, "server is NULL");
-    std::lock_guard<std::mutex> lk(S->mu);
-    auto it = S->meshes.find(mesh_id);
-    if (it == S->meshes.end()) return sfail(TG_ERR_INVALID_ARGUMENT, "unknown or released mesh");
-    std::shared_ptr<Group> g = it->second->g;
-    S->meshes.erase(it);
-    if (g) {
-        g->live--;
-        drop_group_if_unused(S, g);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto it = S->meshes.find(mesh_id);
+        if (it == S->meshes.end())
+            return sfail(TG_ERR_INVALID_ARGUMENT, "unknown or released mesh");
+        std::shared_ptr<Group> g = it->second->g;
+        S->meshes.erase(it);
+        if (g) {
+            g->live--;
+            drop_group_if_unused(S, g);
+        }
     }
+    bury(S);
     return TG_OK;
 }
 
