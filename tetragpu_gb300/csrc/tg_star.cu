@@ -549,24 +549,28 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
                     b.te[6LL * c + pair_slot(sv, t)] = hv_of(S, e, cand_of(t, sv), rs, get4(w, t));
             }
             if (sv <= 1 && (b.tf || b.ft)) {
+                // faces v owns, handled at their first cell: TF of both
+                // cells and FT's second cell, one face id load per face
                 const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
                 for (int o = o_lo; o <= o_hi; o++) {
                     const int ko = cand_of(o, sv);
                     const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
                     const unsigned long long mf = S.cm[e][ka] & S.cm[e][kb];
-                    const int j1 = ctz64(mf);
-                    int of = o;
-                    if (j1 != pos) {
+                    if (ctz64(mf) != pos) continue;
+                    const int fid = rank_of(b.frank, 4LL * c + (3 - o));
+                    if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
+                    const unsigned long long m2 = mf & (mf - 1);
+                    if (!m2) {
+                        if (b.ft) b.ft[2LL * fid + 1] = -1;
+                        continue;
+                    }
+                    const int j2 = rs + ctz64(m2);
+                    const int c2 = S.cell[j2];
+                    if (b.ft) b.ft[2LL * fid + 1] = c2;
+                    if (b.tf) {
                         int x, y;
                         face_others(w, sv, o, x, y);
-                        of = omitted_slot(S.tv[rs + j1], S.vid[e], x, y);
-                    }
-                    const long long q = 4LL * S.cell[rs + j1] + (3 - of);
-                    const int fid = rank_of(b.frank, q);
-                    if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                    if (j1 == pos && b.ft) {
-                        const unsigned long long m2 = mf & (mf - 1);
-                        b.ft[2LL * fid + 1] = m2 ? S.cell[rs + ctz64(m2)] : -1;
+                        b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], S.vid[e], x, y))] = fid;
                     }
                 }
             }
