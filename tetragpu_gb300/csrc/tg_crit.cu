@@ -12,8 +12,8 @@
 //
 // Two kernels, so that a second field on the same mesh reuses the first:
 //   k_crit_adj       field-independent: for every VV entry (v, u), the bitmask
-//                    of v's neighbours adjacent to u.  Thread per VV entry,
-//                    v's row staged in shared memory.
+//                    of v's neighbours adjacent to u.  Thread per edge (both
+//                    of its entries), v's row staged in shared memory.
 //   k_crit_classify  field-dependent: lower/upper split, then a union-find
 //                    with path halving in shared memory over the adjacency
 //                    bits of same-kind neighbours; roots are counted.
@@ -22,26 +22,34 @@
 namespace tg {
 namespace {
 
-// Link adjacency, thread per VV entry (v, u): bit j of the mask is set when
-// v's j-th neighbour is also a neighbour of u.  A block takes the vertices
-// whose VV rows start in a 256-entry window (win), stages those rows in
-// shared memory and scans each u's row from global memory against them.
+// Link adjacency: for every VV entry (v, u), bit j of the mask is set when
+// v's j-th neighbour is also a neighbour of u.  The common neighbours of v
+// and u give both entries (v, u) and (u, v), so one thread takes each edge
+// once, from its lower end v: it scans u's row from global memory, finds each
+// w in v's row (staged in shared memory) by binary search, and sets bit j in
+// (v, u)'s mask and bit i (w's place in u's row) in (u, v)'s, which sits at
+// v's place in u's row.  A block takes the vertices whose VV rows start in a
+// 256-entry window (win); the entries it owns (u > v) form a work list.
 constexpr int kAdjWin = 256;
 constexpr int kAdjCap = kAdjWin + kMaxDeg;
+constexpr int kAdjThreads = 128;
 
-__global__ void __launch_bounds__(kAdjWin)
+__global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
            const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
 {
     __shared__ int nb[kAdjCap];
     __shared__ int meta[kAdjCap];   // row start | row length << 16
-    __shared__ int s_vlo, s_vhi, s_n;
+    __shared__ int vid[kAdjCap];
+    __shared__ int own[kAdjCap];
+    __shared__ int s_vlo, s_vhi, s_n, n_own;
     __shared__ long long s_base;
     if (threadIdx.x == 0) {
         s_vlo = win[blockIdx.x];
         s_vhi = win[blockIdx.x + 1];
         s_base = vv_off[s_vlo];
         s_n = (int)(vv_off[s_vhi] - s_base);
+        n_own = 0;
     }
     __syncthreads();
     const int n = s_n;
@@ -60,29 +68,46 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
             atomicOr(&st->flags, ST_HEAVY_DEG);
             atomicMin(&st->bad_vertex, v);
         }
-        for (int i = 0; i < d; i++) meta[rs + i] = rs | (d << 16);
+        for (int i = 0; i < d; i++) {
+            meta[rs + i] = rs | (d << 16);
+            vid[rs + i] = v;
+        }
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) nb[e] = __ldg(vv + base + e);
     __syncthreads();
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    for (int e = threadIdx.x; e < n; e += blockDim.x)
+        if ((meta[e] >> 16) <= kMaxDeg && nb[e] > vid[e]) own[atomicAdd(&n_own, 1)] = e;
+    __syncthreads();
+    const int no = n_own;
+    for (int k = threadIdx.x; k < no; k += blockDim.x) {
+        const int e = own[k];
         const int m = meta[e], rs = m & 0xffff, d = m >> 16;
-        if (d > kMaxDeg) continue;
         const int *row = nb + rs;
-        const int u = nb[e];
+        const int v = vid[e], u = nb[e];
         const int64_t ub = vv_off[u];
         const int un = (int)(vv_off[u + 1] - ub);
-        unsigned long long bits = 0ull;
+        if (un > kMaxDeg) continue;  // u's own block reports it
+        unsigned long long bits_v = 0ull, bits_u = 0ull;
+        int pv = -1;
 #pragma unroll 4
         for (int i = 0; i < un; i++) {
             const int w = __ldg(vv + ub + i);
+            if (w == v) {
+                pv = i;
+                continue;
+            }
             int lo = 0, hi = d;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
                 if (row[mid] < w) lo = mid + 1; else hi = mid;
             }
-            if (lo < d && row[lo] == w) bits |= 1ull << lo;
+            if (lo < d && row[lo] == w) {
+                bits_v |= 1ull << lo;
+                bits_u |= 1ull << i;
+            }
         }
-        adj[base + e] = bits;
+        adj[base + e] = bits_v;
+        if (pv >= 0) adj[ub + pv] = bits_u;
     }
 }
 
@@ -166,7 +191,7 @@ void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
-    k_crit_adj<<<(unsigned)window_count(n_vv, kAdjWin), kAdjWin, 0, s>>>(
+    k_crit_adj<<<(unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s>>>(
         vv_off, vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
 }
 
