@@ -106,9 +106,9 @@ struct StageM {
     unsigned long long cm[kCap][3];     // star positions holding each candidate
     int hv[kCap][3];                    // at first sightings: list index, then edge id
     int cnt[kCap];
-    int list_u[3 * kCap];
-    int list_id[3 * kCap];
-    int work[3 * kCap];                 // first sightings (entry << 2 | candidate): n_owned
+    int list_u[3 * kCap];               // neighbours, then (after pass 2) their edge ids
+    int work[3 * kCap];                 // first sightings (list index << 11 | entry << 2 |
+                                        // candidate): n_owned
                                         // owned ones (u > v) from the front, n_work others
                                         // from the back
     int n, vlo, vhi, n_work, n_owned;
@@ -267,11 +267,14 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_star_a(StarA a)
+__global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
 {
     __shared__ Stage S;
-    __shared__ int work[3 * kCap];      // first sightings of owned edges (entry << 2 | candidate)
     __shared__ int n_work;
+    // first sightings of owned edges (entry << 2 | candidate), in the hash
+    // keys' space: after the table is built only its masks are read
+    static_assert(sizeof(S.hkey) >= 3 * kCap * sizeof(int), "work list does not fit the keys");
+    int *work = reinterpret_cast<int *>(S.hkey);
     if (!stage_and_hash(S, a.pofs, a.win, a.vorder, a.vtp, a.tvs, a.st)) return;
     const int n = S.n;
     if (threadIdx.x == 0) n_work = 0;
@@ -401,7 +404,7 @@ __device__ __forceinline__ int hv_of(const StageM &S, int e, int k, int rs, int 
     return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
 }
 
-__global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
+__global__ void __launch_bounds__(kThreads, 7) k_star_b(StarB b)
 {
     __shared__ StageM S;
     stage_masks(S, b);
@@ -423,10 +426,11 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
             const int li = atomicAdd(&S.cnt[rs], 1);
             S.list_u[3 * rs + li] = u;
             S.hv[e][k] = li;
+            const int item = (li << 11) | (e << 2) | k;
             if (u > v)
-                S.work[atomicAdd(&S.n_owned, 1)] = (e << 2) | k;
+                S.work[atomicAdd(&S.n_owned, 1)] = item;
             else
-                S.work[3 * kCap - 1 - atomicAdd(&S.n_work, 1)] = (e << 2) | k;
+                S.work[3 * kCap - 1 - atomicAdd(&S.n_work, 1)] = item;
         }
     }
     __syncthreads();
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
     // 2. every first sighting: edge id and VV position
     for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
         const int it = first_item(i);
-        const int e = it >> 2, k = it & 3;
+        const int e = (it >> 2) & 511, k = it & 3;
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m);
         const int t = k + (k >= sv);
@@ -447,12 +451,19 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
         const int *lu = S.list_u + 3 * rs;
         int rank = 0;
         for (int j = 0; j < deg; j++) rank += lu[j] < u;
-        const int id = rank_of(b.erank, 6LL * S.cell[e] + pair_slot(min(sv, t), max(sv, t)));
-        S.list_id[3 * rs + S.hv[e][k]] = id;
-        S.hv[e][k] = id;
+        S.hv[e][k] = rank_of(b.erank, 6LL * S.cell[e] + pair_slot(min(sv, t), max(sv, t)));
         if (b.vv) b.vv[b.vv_off[v] + rank] = u;
     }
     __syncthreads();
+    // the neighbour lists become edge-id lists (for the id order of EE)
+    if (b.eid_sorted) {
+        for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
+            const int it = first_item(i);
+            const int e = (it >> 2) & 511, k = it & 3;
+            S.list_u[3 * m_rs(S.meta[e]) + (it >> 11)] = S.hv[e][k];
+        }
+        __syncthreads();
+    }
 
     // 3a. the edges v owns, four lanes to an edge, the lanes of an edge
     //     taking its cells four at a time in ascending order: ET rows (cells
@@ -468,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
             int rs = 0, u = 0, id = 0;
             unsigned long long mu = 0;
             if (act) {
-                const int e = S.work[i] >> 2, k = S.work[i] & 3;
+                const int e = (S.work[i] >> 2) & 511, k = S.work[i] & 3;
                 const int m = S.meta[e];
                 rs = m_rs(m);
                 u = get4(S.tv[e], k + (k >= m_sv(m)));
@@ -576,11 +587,11 @@ __global__ void __launch_bounds__(kThreads) k_star_b(StarB b)
             }
         } else {
             const int it = first_item(i - n);
-            const int e = it >> 2, k = it & 3;
+            const int e = (it >> 2) & 511, k = it & 3;
             const int rs = m_rs(S.meta[e]);
             const int id = S.hv[e][k];
             const int deg = S.cnt[rs];
-            const int *li = S.list_id + 3 * rs;
+            const int *li = S.list_u + 3 * rs;
             int r = 0;
             for (int j = 0; j < deg; j++) r += li[j] < id;
             b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
