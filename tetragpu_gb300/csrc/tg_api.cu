@@ -232,7 +232,8 @@ struct tg_mesh {
     int32_t *vorder = nullptr;          // [V] vertex at each position (cell-less ones last)
     int64_t *pofs = nullptr;            // [V + 1] VT offsets in that order
     int32_t *vtp = nullptr;             // [4T] VT rows in that order
-    int32_t *st_win = nullptr;          // window table over pofs
+    int32_t *st_win = nullptr;          // window table over pofs (star pass A)
+    int32_t *st_win_b = nullptr;        // the same for star pass B's windows
     // segments of cells (the meshes of a batch): cell starts, and after each
     // extraction their first edge and face ids (device, n_seg + 1 each)
     int64_t n_seg = 0;
@@ -462,7 +463,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             if (T == 0) CK(cudaMemsetAsync(ff_off, 0, 8, s));
         }
         StarB b{};
-        b.pofs = m->pofs; b.win = m->st_win; b.vorder = m->vorder; b.vtp = m->vtp;
+        b.pofs = m->pofs; b.win = m->st_win_b; b.vorder = m->vorder; b.vtp = m->vtp;
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
@@ -608,6 +609,7 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     if (m->pofs) cudaFreeAsync(m->pofs, s);
     if (m->vtp) cudaFreeAsync(m->vtp, s);
     if (m->st_win) cudaFreeAsync(m->st_win, s);
+    if (m->st_win_b) cudaFreeAsync(m->st_win_b, s);
     if (m->seg_c) cudaFreeAsync(m->seg_c, s);
     if (m->seg_ef) cudaFreeAsync(m->seg_ef, s);
     if (m->cadj) cudaFreeAsync(m->cadj, s);
@@ -679,6 +681,8 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
         launch_vtp_fill(m->vorder, m->pofs, V, vt_off, vt, m->vtp, s);
         TRY(dalloc(&m->st_win, window_count(4 * T, star_window()) + 1, s));
         launch_window_starts(m->pofs, V, 4 * T, star_window(), m->st_win, s);
+        TRY(dalloc(&m->st_win_b, window_count(4 * T, star_window_b()) + 1, s));
+        launch_window_starts(m->pofs, V, 4 * T, star_window_b(), m->st_win_b, s);
     }
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);

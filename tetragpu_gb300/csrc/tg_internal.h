@@ -87,7 +87,8 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
 int64_t window_count(int64_t n_entries, int win_size);
 void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int win_size,
                           int32_t *win, cudaStream_t s);
-int star_window();  // the window size of the star kernels over VT
+int star_window();    // the window size of star pass A over VT
+int star_window_b();  // the window size of star pass B
 // sort every VT row (tg_star.cu): window-staged, coalesced.  Also marks each
 // vertex's star-order key 4 * (lowest cell) + (slot in it) in vflag (4T bits,
 // zeroed by the caller) and stores it in vkey[v]; rows with no cells are left
@@ -138,7 +139,7 @@ void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *b
 
 struct StarB {
     const int64_t *pofs;       // as in StarA
-    const int32_t *win;
+    const int32_t *win;        // window table over pofs with star_window_b()
     const int32_t *vorder;
     const int32_t *vtp;
     const int4 *tvs;

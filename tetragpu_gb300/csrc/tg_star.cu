@@ -46,6 +46,13 @@ namespace {
 #endif
 constexpr int kWin = TG_STAR_WIN;         // VT entries per block window
 constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in the window)
+// pass B stages less per entry (no hash), so smaller windows let eight of its
+// blocks share an SM
+#ifndef TG_STAR_WIN_B
+#define TG_STAR_WIN_B 224
+#endif
+constexpr int kWinB = TG_STAR_WIN_B;
+constexpr int kCapB = kWinB + kMaxStar;
 constexpr int kThreads = TG_STAR_THREADS;
 constexpr int kHashBits = TG_STAR_HASH_BITS;
 constexpr int kHash = 1 << kHashBits;     // (vertex, neighbour) slots per block, >= 3 * kCap
@@ -99,15 +106,15 @@ static_assert(sizeof(Stage) <= 48 * 1024, "star stage exceeds the static shared-
 // vertex's neighbours (at 3 * row start, the most a row of D cells can have
 // is 3D) with their edge ids.
 struct StageM {
-    int cell[kCap];
-    int4 tv[kCap];
-    int vid[kCap];
-    int meta[kCap];                     // row start | D << 10 | slot of v << 20
-    unsigned long long cm[kCap][3];     // star positions holding each candidate
-    int hv[kCap][3];                    // at first sightings: list index, then edge id
-    int cnt[kCap];
-    int list_u[3 * kCap];               // neighbours, then (after pass 2) their edge ids
-    int work[3 * kCap];                 // first sightings (list index << 11 | entry << 2 |
+    int cell[kCapB];
+    int4 tv[kCapB];
+    int vid[kCapB];
+    int meta[kCapB];                     // row start | D << 10 | slot of v << 20
+    unsigned long long cm[kCapB][3];     // star positions holding each candidate
+    int hv[kCapB][3];                    // at first sightings: list index, then edge id
+    int cnt[kCapB];
+    int list_u[3 * kCapB];               // neighbours, then (after pass 2) their edge ids
+    int work[3 * kCapB];                 // first sightings (list index << 11 | entry << 2 |
                                         // candidate): n_owned
                                         // owned ones (u > v) from the front, n_work others
                                         // from the back
@@ -404,7 +411,7 @@ __device__ __forceinline__ int hv_of(const StageM &S, int e, int k, int rs, int 
     return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
 }
 
-__global__ void __launch_bounds__(kThreads, 7) k_star_b(StarB b)
+__global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
 {
     __shared__ StageM S;
     stage_masks(S, b);
@@ -430,13 +437,13 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_b(StarB b)
             if (u > v)
                 S.work[atomicAdd(&S.n_owned, 1)] = item;
             else
-                S.work[3 * kCap - 1 - atomicAdd(&S.n_work, 1)] = item;
+                S.work[3 * kCapB - 1 - atomicAdd(&S.n_work, 1)] = item;
         }
     }
     __syncthreads();
     const int n_owned = S.n_owned, n_first = n_owned + S.n_work;
     auto first_item = [&](int i) {
-        return i < n_owned ? S.work[i] : S.work[3 * kCap - 1 - (i - n_owned)];
+        return i < n_owned ? S.work[i] : S.work[3 * kCapB - 1 - (i - n_owned)];
     };
 
     // 2. every first sighting: edge id and VV position
@@ -976,10 +983,12 @@ k_seg_ranks(const int64_t *__restrict__ seg_c, int64_t n, const uint2 *__restric
 }
 
 inline unsigned n_windows(int64_t nvt) { return (unsigned)(nvt / kWin + 1); }
+inline unsigned n_windows_b(int64_t nvt) { return (unsigned)(nvt / kWinB + 1); }
 
 }  // namespace
 
 int star_window() { return kWin; }
+int star_window_b() { return kWinB; }
 
 int64_t window_count(int64_t n_entries, int win_size) { return n_entries / win_size + 1; }
 
@@ -1039,7 +1048,7 @@ void launch_star_b(const StarB &b, cudaStream_t s)
 {
     if (b.V == 0) return;
     Launch L("k_star_b", s);
-    k_star_b<<<n_windows(b.nvt), kThreads, 0, s>>>(b);
+    k_star_b<<<n_windows_b(b.nvt), kThreads, 0, s>>>(b);
 }
 
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
