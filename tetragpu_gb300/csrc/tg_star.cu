@@ -9,24 +9,26 @@
 // which is what the reference CPU ids are ranks of (src/cpu_extraction.cpp:
 // 28-62 edges, 122-174 faces).
 //
-// Work decomposition: VT is cut into windows of kWin entries.  A block owns
-// the vertices whose rows START in its window (at most kWin + kMaxStar - 1
-// entries), stages their cells and the cells' sorted TV rows in shared
-// memory (all gathers in flight at once), and gives one thread to each
-// (vertex, star cell) entry.  A shared-memory hash keyed by (vertex,
-// neighbour) holds, per neighbour, the 64-bit mask of star positions whose
-// cell contains it; lanes holding the same key are merged by
-// __match_any_sync first, so one lane per group touches the table.  With the
-// masks, "first position holding u" is a count-trailing-zeros and "first
-// position holding x and y" a ctz of an AND.
+// Work decomposition: the VT rows, in star processing order (vertices by
+// first cell, see k_vorder_place), are cut into windows of kWin entries (kWinB
+// for pass B).  A block owns the vertices whose rows START in its window (at
+// most kWin + kMaxStar - 1 entries), stages their cells and the cells' sorted
+// TV rows in shared memory (all gathers in flight at once), and gives one
+// thread to each (vertex, star cell) entry.  In pass A a shared-memory hash
+// keyed by (vertex, neighbour) holds, per neighbour, the 64-bit mask of star
+// positions whose cell contains it; lanes holding the same key are merged by
+// __match_any_sync first, so one lane per group touches the table.  Pass A
+// leaves every entry's three candidate masks in global memory and pass B
+// stages them instead of rebuilding the table.  With the masks, "first
+// position holding u" is a count-trailing-zeros and "first position holding
+// x and y" a ctz of an AND.
 //
 //   k_star_a  first-occurrence bitmaps (edges owned by v = v is the low end,
 //             faces owned by v = v is the lowest vertex, boundary faces), the
 //             ET / EF row lengths at each owned edge's first-occurrence slot,
-//             and neighbour counts
-//   k_star_b  ids (ranks of first occurrences), sorted VV rows, incident edge
-//             ids (by neighbour and by id), TE, TF, FT's second cell, ET and
-//             EF rows
+//             neighbour counts, the candidate masks
+//   k_star_b  ids (ranks of first occurrences), sorted VV rows, id-sorted
+//             incident edge ids, TE, TF, FT's second cell, ET and EF rows
 //   k_edge_offsets_* / k_face_slots  the id-ordered passes over occurrence
 //             slots: ET / EF / EE offsets and EV; FV, FT's first cell, FF
 //             offsets
