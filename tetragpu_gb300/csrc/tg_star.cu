@@ -54,6 +54,12 @@ constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in th
 #define TG_STAR_WIN_B 224
 #endif
 constexpr int kWinB = TG_STAR_WIN_B;
+#ifndef TG_EF_LANES
+#define TG_EF_LANES 2
+#endif
+constexpr int kEfLanes = TG_EF_LANES;     // lanes per owned edge for its ET / EF rows
+static_assert(kEfLanes == 1 || kEfLanes == 2 || kEfLanes == 4 || kEfLanes == 8,
+              "lanes per edge: 1, 2, 4 or 8");
 constexpr int kCapB = kWinB + kMaxStar;
 constexpr int kThreads = TG_STAR_THREADS;
 constexpr int kHashBits = TG_STAR_HASH_BITS;
@@ -474,16 +480,17 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
         __syncthreads();
     }
 
-    // 3a. the edges v owns, four lanes to an edge, the lanes of an edge
-    //     taking its cells four at a time in ascending order: ET rows (cells
-    //     of the star holding u, ascending) and EF rows (faces (v,u,x) at
-    //     their first cell, cells ascending, two faces of one cell by column:
-    //     ascending first occurrence, which is ascending face id); a scan
-    //     over the four lanes places each cell's faces
+    // 3a. the edges v owns, kEfLanes lanes to an edge, the lanes of an edge
+    //     taking its cells kEfLanes at a time in ascending order: ET rows
+    //     (cells of the star holding u, ascending) and EF rows (faces (v,u,x)
+    //     at their first cell, cells ascending, two faces of one cell by
+    //     column: ascending first occurrence, which is ascending face id); a
+    //     scan over the lanes places each cell's faces
     if (b.et || b.ef) {
-        const int span = ((n_owned * 4 + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+        constexpr int L = kEfLanes;
+        const int span = ((n_owned * L + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
         for (int t = threadIdx.x; t < span; t += blockDim.x) {   // block-uniform trip count
-            const int i = t >> 2, sub = t & 3;
+            const int i = t / L, sub = t % L;
             const bool act = i < n_owned;
             int rs = 0, u = 0, id = 0;
             unsigned long long mu = 0;
@@ -495,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
                 mu = S.cm[e][k];
                 id = S.hv[e][k];
             }
-            const int rounds = (__popcll(mu) + 3) >> 2;
+            const int rounds = (__popcll(mu) + L - 1) / L;
             const int max_rounds = __reduce_max_sync(0xffffffffu, rounds);
             long long et_p = act && b.et ? b.et_off[id] : 0;
             long long ef_p = act && b.ef ? b.ef_off[id] : 0;
@@ -531,22 +538,21 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
                     q0 = 4LL * S.cell[ej];
                 }
                 int x = nf;
-                int y = __shfl_up_sync(0xffffffffu, x, 1, 4);
-                if (sub >= 1) x += y;
-                y = __shfl_up_sync(0xffffffffu, x, 2, 4);
-                if (sub >= 2) x += y;
-                const int tot = __shfl_sync(0xffffffffu, x, 3, 4);
+#pragma unroll
+                for (int off = 1; off < L; off <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, off, L);
+                    if (sub >= off) x += y;
+                }
+                const int tot = __shfl_sync(0xffffffffu, x, L - 1, L);
                 if (b.ef && nf > 0) {
                     const long long p = ef_p + (x - nf);
                     b.ef[p] = rank_of(b.frank, q0 + col0);
                     if (nf == 2) b.ef[p + 1] = rank_of(b.frank, q0 + col1);
                 }
-                et_p += 4;
+                et_p += L;
                 ef_p += tot;
-                rest &= rest - 1;
-                rest &= rest - 1;
-                rest &= rest - 1;
-                rest &= rest - 1;
+#pragma unroll
+                for (int q = 0; q < L; q++) rest &= rest - 1;
             }
         }
     }
