@@ -57,7 +57,11 @@ constexpr int kWinB = TG_STAR_WIN_B;
 #ifndef TG_EF_LANES
 #define TG_EF_LANES 2
 #endif
-constexpr int kEfLanes = TG_EF_LANES;     // lanes per owned edge for its ET / EF rows
+constexpr int kEfLanes = TG_EF_LANES;     // lanes per owned edge for its ET / EF rows (pass B)
+#ifndef TG_EFA_LANES
+#define TG_EFA_LANES 2
+#endif
+constexpr int kEfLanesA = TG_EFA_LANES;   // lanes per owned edge for its EF count (pass A)
 static_assert(kEfLanes == 1 || kEfLanes == 2 || kEfLanes == 4 || kEfLanes == 8,
               "lanes per edge: 1, 2, 4 or 8");
 constexpr int kCapB = kWinB + kMaxStar;
@@ -332,33 +336,47 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
         }
     }
     __syncthreads();
-    // the edges v owns, one per thread: flag the first occurrence and record
-    // the ET and EF row lengths at that occurrence slot.  A face (v,u,x) is
-    // counted in the first cell holding u and x.
+    // the edges v owns, kEfLanesA lanes to an edge (each lane every
+    // kEfLanesA-th cell of the edge's star): flag the first occurrence and
+    // record the ET and EF row lengths at that occurrence slot.  A face
+    // (v,u,x) is counted in the first cell holding u and x.
     const int nw = n_work;
-    for (int i = threadIdx.x; i < nw; i += blockDim.x) {
-        const int e = work[i] >> 2, k = work[i] & 3;
-        const int m = S.meta[e];
-        const int rs = m_rs(m), sv = m_sv(m);
-        const int t = k + (k >= sv);
-        const int u = get4(S.tv[e], t);
-        const unsigned long long mu = S.hmask[S.cslot[e][k]];
-        const long long p = 6LL * S.cell[e] + pair_slot(sv, t);
-        set_bit(a.eflag, p);
+    constexpr int L = kEfLanesA;
+    const int span = ((nw * L + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
+    for (int tt = threadIdx.x; tt < span; tt += blockDim.x) {   // block-uniform trip count
+        const int i = tt / L, sub = tt % L;
         int n_ef = 0;
-        for (unsigned long long mm = mu; mm; mm &= mm - 1) {
-            const int j = ctz64(mm);
-            const int ej = rs + j;
-            const int4 wj = S.tv[ej];
-            const int sj = m_sv(S.meta[ej]);
-            const int ku = cand_of(slot_of(wj, u), sj);
+        unsigned long long mu = 0;
+        long long p = 0;
+        if (i < nw) {
+            const int e = work[i] >> 2, k = work[i] & 3;
+            const int m = S.meta[e];
+            const int rs = m_rs(m), sv = m_sv(m);
+            const int t = k + (k >= sv);
+            const int u = get4(S.tv[e], t);
+            mu = S.hmask[S.cslot[e][k]];
+            p = 6LL * S.cell[e] + pair_slot(sv, t);
+            unsigned long long mm = mu;
+            for (int q = 0; q < sub; q++) mm &= mm - 1;
+            while (mm) {
+                const int j = ctz64(mm);
+                const int ej = rs + j;
+                const int ku = cand_of(slot_of(S.tv[ej], u), m_sv(S.meta[ej]));
 #pragma unroll
-            for (int kk = 0; kk < 3; kk++) {
-                if (kk == ku) continue;
-                n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk == ku) continue;
+                    n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
+                }
+#pragma unroll
+                for (int q = 0; q < L; q++) mm &= mm - 1;
             }
         }
-        a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+#pragma unroll
+        for (int off = 1; off < L; off <<= 1) n_ef += __shfl_xor_sync(0xffffffffu, n_ef, off);
+        if (i < nw && sub == 0) {
+            set_bit(a.eflag, p);
+            a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+        }
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
