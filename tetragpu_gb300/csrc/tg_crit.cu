@@ -30,12 +30,18 @@ namespace {
 // (v, u)'s mask and bit i (w's place in u's row) in (u, v)'s, which sits at
 // v's place in u's row.  A block takes the vertices whose VV rows start in a
 // 256-entry window (win); the entries it owns (u > v) form a work list.
-constexpr int kAdjWin = 256;
+#ifndef TG_ADJ_WIN
+#define TG_ADJ_WIN 256
+#endif
+#ifndef TG_ADJ_THREADS
+#define TG_ADJ_THREADS 128
+#endif
+constexpr int kAdjWin = TG_ADJ_WIN;
 constexpr int kAdjCap = kAdjWin + kMaxDeg;
-constexpr int kAdjThreads = 128;
+constexpr int kAdjThreads = TG_ADJ_THREADS;
 
 __global__ void __launch_bounds__(kAdjThreads)
-k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
+k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
            const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
 {
     __shared__ int nb[kAdjCap];
@@ -84,26 +90,47 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
         const int m = meta[e], rs = m & 0xffff, d = m >> 16;
         const int *row = nb + rs;
         const int v = vid[e], u = nb[e];
+        const bool vec = (reinterpret_cast<uintptr_t>(vv) & 15) == 0;
         const int64_t ub = vv_off[u];
         const int un = (int)(vv_off[u + 1] - ub);
         if (un > kMaxDeg) continue;  // u's own block reports it
         unsigned long long bits_v = 0ull, bits_u = 0ull;
         int pv = -1;
-#pragma unroll 4
-        for (int i = 0; i < un; i++) {
-            const int w = __ldg(vv + ub + i);
-            if (w == v) {
-                pv = i;
-                continue;
+        // u's row read four entries at a time from 16-byte boundaries (one
+        // load instruction per four entries; the rows of a warp's lanes lie
+        // apart, so each load costs a memory transaction per lane), scalar
+        // loads for a last group that would end past the array, or when the
+        // caller's VV array itself is not 16-byte aligned
+        for (int64_t a0 = ub & ~3LL; a0 < ub + un; a0 += 4) {
+            int q[4];
+            if (vec && a0 + 4 <= n_vv) {
+                const int4 x = __ldg(reinterpret_cast<const int4 *>(vv + a0));
+                q[0] = x.x;
+                q[1] = x.y;
+                q[2] = x.z;
+                q[3] = x.w;
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; t++) q[t] = a0 + t < n_vv ? __ldg(vv + a0 + t) : 0;
             }
-            int lo = 0, hi = d;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (row[mid] < w) lo = mid + 1; else hi = mid;
-            }
-            if (lo < d && row[lo] == w) {
-                bits_v |= 1ull << lo;
-                bits_u |= 1ull << i;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int i = (int)(a0 + t - ub);
+                if (i < 0 || i >= un) continue;
+                const int w = q[t];
+                if (w == v) {
+                    pv = i;
+                    continue;
+                }
+                int lo = 0, hi = d;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (row[mid] < w) lo = mid + 1; else hi = mid;
+                }
+                if (lo < d && row[lo] == w) {
+                    bits_v |= 1ull << lo;
+                    bits_u |= 1ull << i;
+                }
             }
         }
         adj[base + e] = bits_v;
@@ -192,7 +219,7 @@ void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv
     if (V == 0) return;
     Launch L("k_crit_adj", s);
     k_crit_adj<<<(unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s>>>(
-        vv_off, vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
+        vv_off, vv, n_vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
