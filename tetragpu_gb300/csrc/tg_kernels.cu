@@ -313,57 +313,64 @@ __device__ __forceinline__ void ee_merge_one(const int *__restrict__ eid, int64_
 }
 
 // Rows of at most 16 entries each (the common case: 14 neighbours inside a
-// Kuhn grid) go four edges at a time, eight lanes to an edge, four
-// registers to a lane (position gl + 8 r): the same bitonic merge over 32
-// positions with two register stages and three shuffle stages.
+// Kuhn grid) go 32 / G edges at a time, G lanes to an edge, 32 / G registers
+// to a lane (position gl + G r): the same bitonic merge over 32 positions,
+// the strides of G and more between registers, the smaller ones between the
+// group's lanes.
+#ifndef TG_EE_GROUP
+#define TG_EE_GROUP 4
+#endif
+constexpr int kEeGroup = TG_EE_GROUP;
+static_assert(kEeGroup == 4 || kEeGroup == 8, "lanes per edge: 4 or 8");
+
+template <int G>
 __device__ __forceinline__ void ee_merge_group(const int *__restrict__ eid, int64_t ra, int na,
                                                int64_t rb, int nb, int ei, int *__restrict__ out,
                                                int gl, int g)
 {
-    int x[4];
+    constexpr int R = 32 / G;
+    int x[R];
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int p = gl + 8 * r;
-        if (r < 2) {
+    for (int r = 0; r < R; r++) {
+        const int p = gl + G * r;
+        if (p < 16) {
             x[r] = p < na ? __ldg(eid + ra + p) : INT_MAX;
         } else {
             const int j = 31 - p;
             x[r] = j < nb ? __ldg(eid + rb + j) : INT_MAX;
         }
     }
-    // stride 16: registers r, r + 2; stride 8: r, r + 1
+    // strides 16 .. G: between registers (register stride sr = stride / G)
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-        const int lo = min(x[r], x[r + 2]), hi = max(x[r], x[r + 2]);
-        x[r] = lo;
-        x[r + 2] = hi;
+    for (int sr = 16 / G; sr >= 1; sr >>= 1) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            if (r & sr) continue;
+            const int lo = min(x[r], x[r + sr]), hi = max(x[r], x[r + sr]);
+            x[r] = lo;
+            x[r + sr] = hi;
+        }
     }
+    // strides G / 2 .. 1: lanes of the group
 #pragma unroll
-    for (int r = 0; r < 4; r += 2) {
-        const int lo = min(x[r], x[r + 1]), hi = max(x[r], x[r + 1]);
-        x[r] = lo;
-        x[r + 1] = hi;
-    }
-    // strides 4, 2, 1: lanes of the group
-#pragma unroll
-    for (int sl = 4; sl >= 1; sl >>= 1) {
+    for (int sl = G / 2; sl >= 1; sl >>= 1) {
         const bool upper = gl & sl;
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
+        for (int r = 0; r < R; r++) {
             const int y = __shfl_xor_sync(kFull, x[r], sl);
             x[r] = upper ? max(x[r], y) : min(x[r], y);
         }
     }
     int pe = 32;
 #pragma unroll
-    for (int r = 3; r >= 0; r--) {
-        const unsigned m = (__ballot_sync(kFull, x[r] == ei) >> (8 * g)) & 0xffu;
-        if (m) pe = 8 * r + __ffs(m) - 1;
+    for (int r = R - 1; r >= 0; r--) {
+        const unsigned m = (__ballot_sync(kFull, x[r] == ei) >> (G * g)) & ((1u << G) - 1u);
+        if (m) pe = G * r + __ffs(m) - 1;
     }
     const int n = na + nb;
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int p = gl + 8 * r;
+    for (int r = 0; r < R; r++) {
+        const int p = gl + G * r;
         if (p < n && x[r] != ei) out[p - (p > pe ? 2 : 0)] = x[r];
     }
 }
@@ -388,17 +395,18 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
     }
     const unsigned small = __ballot_sync(kFull, lane < cnt && max(my_na, my_nb) <= 16);
     const unsigned big = __ballot_sync(kFull, lane < cnt) & ~small;
-    // small edges, four per round (group g takes the (4 k + g)-th one)
-    const int g = lane >> 3, gl = lane & 7;
+    // small edges, 32 / G per round (group g takes the (k + g)-th one)
+    constexpr int G = kEeGroup;
+    const int g = lane / G, gl = lane % G;
     const int n_small = __popc(small);
-    for (int k = 0; k < n_small; k += 4) {
+    for (int k = 0; k < n_small; k += 32 / G) {
         const int which = k + g;
         const int src = which < n_small ? (int)__fns(small, 0, which + 1) : 0;
         const int64_t ra = __shfl_sync(kFull, my_ra, src), rb = __shfl_sync(kFull, my_rb, src);
         int na = __shfl_sync(kFull, my_na, src), nb = __shfl_sync(kFull, my_nb, src);
         const int64_t o = __shfl_sync(kFull, my_out, src);
         if (which >= n_small) na = nb = 0;  // an idle group: nothing to write
-        ee_merge_group(eid, ra, na, rb, nb, (int)(e0 + src), ee + o, gl, g);
+        ee_merge_group<G>(eid, ra, na, rb, nb, (int)(e0 + src), ee + o, gl, g);
     }
     // longer rows one edge at a time over the whole warp
     for (unsigned rest = big; rest; rest &= rest - 1) {
