@@ -36,44 +36,10 @@ __device__ __forceinline__ int get4(const int4 &w, int i)
     return i == 0 ? w.x : (i == 1 ? w.y : (i == 2 ? w.z : w.w));
 }
 
-// position of u in a sorted row that contains it
-__device__ __forceinline__ int slot_of(const int4 &w, int u)
-{
-    return (w.x < u) + (w.y < u) + (w.z < u) + (w.w < u);
-}
-
 // index of the vertex pair (s, t), s < t, in the reference TE order
 __device__ __forceinline__ int pair_slot(int s, int t)
 {
     return s == 0 ? t - 1 : (s == 1 ? t + 1 : 5);
-}
-
-// slot of the one vertex of sorted row w that is none of a, b, c
-__device__ __forceinline__ int omitted_slot(const int4 &w, int a, int b, int c)
-{
-    if (w.x != a && w.x != b && w.x != c) return 0;
-    if (w.y != a && w.y != b && w.y != c) return 1;
-    if (w.z != a && w.z != b && w.z != c) return 2;
-    return 3;
-}
-
-// rank of occurrence p among the set bits of flag (ids are ranks)
-__device__ __forceinline__ int bit_rank(const uint32_t *__restrict__ flag,
-                                        const int32_t *__restrict__ pre, long long p)
-{
-    const long long wd = p >> 5;
-    const uint32_t bits = __ldg(flag + wd);
-    return __ldg(pre + wd) + __popc(bits & ((1u << (p & 31)) - 1u));
-}
-
-__device__ __forceinline__ int lower_bound_sm(const int *a, int n, int key)
-{
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int m = (lo + hi) >> 1;
-        if (a[m] < key) lo = m + 1; else hi = m;
-    }
-    return lo;
 }
 
 #define TG_CSWAP(x, y) \
