@@ -891,15 +891,14 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets 
     const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
     long long x[3] = {0, 0, 0};
     const uint32_t bits = slot_bits8(p, s0);
-    int et[8], ef[8], ee[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        et[i] = ef[i] = ee[i] = 0;
-        if (!((bits >> i) & 1u) || s0 + i >= p.n_slots) continue;
-        slot_counts(p, s0 + i, et[i], ef[i], ee[i]);
-        x[0] += et[i];
-        x[1] += ef[i];
-        x[2] += ee[i];
+    for (uint32_t m = bits; m; m &= m - 1) {
+        const int i = __ffs(m) - 1;
+        if (s0 + i >= p.n_slots) break;
+        int et, ef, ee;
+        slot_counts(p, s0 + i, et, ef, ee);
+        x[0] += et;
+        x[1] += ef;
+        x[2] += ee;
     }
     long long excl[3], tot[3];
     block_scan3(x, excl, tot);
@@ -907,11 +906,13 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets 
     for (int q = 0; q < 3; q++) run[q] = p.partials[3 * blockIdx.x + q] + excl[q];
     if (!bits) return;
     int id = rank_of(erank, s0);
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        if (!((bits >> i) & 1u)) continue;
+    // the counts again (their loads hit the cache): registers for eight
+    // slots' counts would halve the blocks an SM holds
+    for (uint32_t m = bits; m; m &= m - 1) {
+        const int i = __ffs(m) - 1;
+        const long long s = s0 + i;
         if (p.ev) {
-            const long long s = s0 + i, cell = s / 6;
+            const long long cell = s / 6;
             const int j = (int)(s - 6 * cell);
             const int4 w = __ldg(p.tvs + cell);
             const int ia = j < 3 ? 0 : (j < 5 ? 1 : 2);
@@ -921,9 +922,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets 
         if (p.et_off) p.et_off[id] = run[0];
         if (p.ef_off) p.ef_off[id] = run[1];
         if (p.ee_off) p.ee_off[id] = run[2];
-        run[0] += et[i];
-        run[1] += ef[i];
-        run[2] += ee[i];
+        int et, ef, ee;
+        slot_counts(p, s, et, ef, ee);
+        run[0] += et;
+        run[1] += ef;
+        run[2] += ee;
         id++;
     }
 }
