@@ -975,7 +975,7 @@ k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__r
 // VT rows copied into processing order: a warp fetches 32 rows' positions
 // and sources at once, then copies them one after another, lanes across the
 // row
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
 k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int64_t V,
            const int64_t *__restrict__ vt_off, const int *__restrict__ vt, int *__restrict__ vtp)
 {
