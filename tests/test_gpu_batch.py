@@ -93,3 +93,23 @@ def test_batch_of_nothing(gpu_lib):
     with gpu_lib.Batch([], []) as b:
         b.extract(gpu_lib.ALL_RELATIONS)
         assert b.n_meshes == 0
+
+
+def test_uneven_batch_matches_meshes_alone(gpu_lib):
+    """Forty meshes from the uneven-batch generator (sizes log-uniform, 0-30%
+    coned, ids permuted): every mesh's relations and classes from the batch
+    equal the mesh processed alone, compared by digest."""
+    from helpers import digest
+    meshes = meshgen.workload_batch(n_meshes=40, lo=2000, hi=60000, seed=91)
+    field = np.concatenate([m.field for m in meshes])
+    with gpu_lib.Batch([m.tv for m in meshes], [m.n_verts for m in meshes]) as b:
+        b.extract(gpu_lib.ALL_RELATIONS)
+        classes = b.critical_points(field)
+        v0 = 0
+        for i, m in enumerate(meshes):
+            with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+                g.extract(gpu_lib.ALL_RELATIONS)
+                for n in RELS:
+                    assert digest(b.relation(i, n)) == digest(g.relation(n)), (i, n)
+                assert np.array_equal(classes[v0:v0 + m.n_verts], g.critical_points(m.field))
+            v0 += m.n_verts
