@@ -438,7 +438,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         // id-ordered passes over the occurrence slots
         if (et_off || ef_off || ee_off || ev) {
             char *scratch2;
-            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T) + 256));
+            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T, E) + 256));
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
                                 ev, scratch2, s);
         }

@@ -126,7 +126,7 @@ void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const
                       int64_t *seg_ef, cudaStream_t s);
 
 // ET / EF / EE offsets in edge-id order from one scan over the 6T edge slots
-size_t edge_offsets_scratch_bytes(int64_t n_slots);
+size_t edge_offsets_scratch_bytes(int64_t n_slots, int64_t E);
 // (also writes EV when ev is given)
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,

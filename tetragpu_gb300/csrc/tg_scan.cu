@@ -95,16 +95,30 @@ __global__ void __launch_bounds__(1024) k_scan_partials(ScanParams p)
     const int64_t ntiles = (j.n + kTile - 1) / kTile;
     int64_t *part = p.partials[jb];
     __shared__ int64_t sm[1024 / 32 + 1];
+    // chunks of 8192 tiles: a thread loads eight consecutive partials at
+    // once, one block-wide scan of the thread sums per chunk
+    constexpr int kPer = 8;
     int64_t carry = 0;
-    for (int64_t b = 0; b < ntiles; b += 1024) {
-        const int64_t i = b + threadIdx.x;
-        int64_t x = (i < ntiles) ? part[i] : 0;
-        int64_t excl;
-        int64_t total = block_exclusive_scan<1024>(x, excl, sm);
-        if (i < ntiles) part[i] = carry + excl;
-        carry += total;
+    for (int64_t b = 0; b < ntiles; b += 1024 * kPer) {
+        const int64_t i0 = b + (int64_t)threadIdx.x * kPer;
+        int64_t v[kPer], x = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            v[k] = i0 + k < ntiles ? part[i0 + k] : 0;
+            x += v[k];
+        }
+        int64_t run;
+        const int64_t tot = block_exclusive_scan<1024>(x, run, sm);
+        run += carry;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            if (i0 + k < ntiles) part[i0 + k] = run;
+            run += v[k];
+        }
+        carry += tot;
     }
-    if (threadIdx.x == 0) store_value(j, j.n, carry);
+    const int64_t total = carry;
+    if (threadIdx.x == 0) store_value(j, j.n, total);
 }
 
 __global__ void __launch_bounds__(kThreads) k_scan_down(ScanParams p)

@@ -749,42 +749,37 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
 // occurrences, so scanning the 6T edge-occurrence slots in order visits the
 // edges in id order: a slot holding a first occurrence contributes the ET
 // and EF row lengths k_star_a left there and deg(a) + deg(b) - 2 for EE.
+// The reduce pass visits a tile's slots, records every edge's three lengths
+// (one packed word per edge id) and EV, and sums them per tile; the down pass
+// scans the packed words of the same tile's id range (ids are contiguous
+// over a slot range), so it gathers nothing.
+#ifndef TG_EDGE_ITEMS
+#define TG_EDGE_ITEMS 8
+#endif
 constexpr int kEdgeThreads = 256;
-constexpr int kEdgeTile = 8 * kEdgeThreads;   // slots per tile, 8 per thread
+constexpr int kEdgeItems = TG_EDGE_ITEMS;             // slots per thread: 8, 16 or 32
+constexpr int kEdgeTile = kEdgeItems * kEdgeThreads;  // slots per tile
+static_assert(kEdgeItems == 8 || kEdgeItems == 16 || kEdgeItems == 32, "slots per thread");
 
 struct EdgeOffsets {
     const uint32_t *eflag;
     const unsigned short *ecnt;
     const int4 *tvs;
     const int32_t *deg;
+    const uint2 *erank;
     int64_t n_slots;
     int64_t *partials;   // 3 per tile
+    uint32_t *len;       // [E]: ET | EF << 8 | EE << 16
     int64_t *et_off, *ef_off, *ee_off;
     int32_t *ev;         // [2E] or null: the edge's two vertices, ascending
     int64_t E;
 };
 
-__device__ __forceinline__ void slot_counts(const EdgeOffsets &p, long long s, int &et, int &ef,
-                                            int &ee)
-{
-    const unsigned short c = p.ecnt[s];
-    et = c & 0xff;
-    ef = c >> 8;
-    if (p.ee_off) {
-        const long long cell = s / 6;
-        const int j = (int)(s - 6 * cell);
-        const int4 w = __ldg(p.tvs + cell);
-        const int ia = j < 3 ? 0 : (j < 5 ? 1 : 2);
-        const int ib = j < 3 ? j + 1 : (j == 3 ? 2 : 3);
-        ee = __ldg(p.deg + get4(w, ia)) + __ldg(p.deg + get4(w, ib)) - 2;
-    } else {
-        ee = 0;
-    }
-}
-
+template <int NT>
 __device__ __forceinline__ void block_scan3(long long x[3], long long excl[3], long long tot[3])
 {
-    __shared__ long long sm[3][kEdgeThreads / 32 + 1];
+    static_assert(NT % 32 == 0 && NT <= 1024, "block of whole warps");
+    __shared__ long long sm[3][NT / 32 + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -801,83 +796,96 @@ __device__ __forceinline__ void block_scan3(long long x[3], long long excl[3], l
     if (warp == 0) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const long long w = lane < kEdgeThreads / 32 ? sm[q][lane] : 0;
+            const long long w = lane < NT / 32 ? sm[q][lane] : 0;
             long long wi = w;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const long long y = __shfl_up_sync(0xffffffffu, wi, o);
                 if (lane >= o) wi += y;
             }
-            if (lane < kEdgeThreads / 32) sm[q][lane] = wi - w;
-            if (lane == kEdgeThreads / 32 - 1) sm[q][kEdgeThreads / 32] = wi;
+            if (lane < NT / 32) sm[q][lane] = wi - w;
+            if (lane == NT / 32 - 1) sm[q][NT / 32] = wi;
         }
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 3; q++) {
         excl[q] += sm[q][warp];
-        tot[q] = sm[q][kEdgeThreads / 32];
+        tot[q] = sm[q][NT / 32];
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ uint32_t slot_bits8(const EdgeOffsets &p, long long s0)
+__device__ __forceinline__ uint32_t slot_bits(const EdgeOffsets &p, long long s0)
 {
-    // 8 consecutive slots starting at a multiple of 8 lie in one 32-bit word
-    return s0 < p.n_slots ? (p.eflag[s0 >> 5] >> (s0 & 31)) & 0xffu : 0u;
+    // kEdgeItems consecutive slots starting at a multiple of kEdgeItems lie
+    // in one 32-bit word
+    if (s0 >= p.n_slots) return 0u;
+    const uint32_t w = p.eflag[s0 >> 5];
+    return kEdgeItems == 32 ? w : (w >> (s0 & 31)) & ((1u << kEdgeItems) - 1u);
 }
 
 __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_reduce(EdgeOffsets p)
 {
-    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
+    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * kEdgeItems;
     long long x[3] = {0, 0, 0};
-    const uint32_t bits = slot_bits8(p, s0);
-    for (int i = 0; i < 8; i++) {
-        if (!((bits >> i) & 1u) || s0 + i >= p.n_slots) continue;
-        int et, ef, ee;
-        slot_counts(p, s0 + i, et, ef, ee);
-        x[0] += et;
-        x[1] += ef;
-        x[2] += ee;
+    const uint32_t bits = slot_bits(p, s0);
+    if (bits) {
+        int id = rank_of(p.erank, s0);
+        for (uint32_t m = bits; m; m &= m - 1) {
+            const int i = __ffs(m) - 1;
+            const long long s = s0 + i;
+            if (s >= p.n_slots) break;
+            const long long cell = s / 6;
+            const int j = (int)(s - 6 * cell);
+            const int4 w = __ldg(p.tvs + cell);
+            const int a = get4(w, j < 3 ? 0 : (j < 5 ? 1 : 2));
+            const int b = get4(w, j < 3 ? j + 1 : (j == 3 ? 2 : 3));
+            const unsigned short c = p.ecnt[s];
+            const int et = c & 0xff, ef = c >> 8;
+            const int ee = p.ee_off ? __ldg(p.deg + a) + __ldg(p.deg + b) - 2 : 0;
+            x[0] += et;
+            x[1] += ef;
+            x[2] += ee;
+            p.len[id] = (uint32_t)c | ((uint32_t)ee << 16);
+            if (p.ev) reinterpret_cast<int2 *>(p.ev)[id] = make_int2(a, b);
+            id++;
+        }
     }
     long long excl[3], tot[3];
-    block_scan3(x, excl, tot);
+    block_scan3<kEdgeThreads>(x, excl, tot);
     if (threadIdx.x == 0)
         for (int q = 0; q < 3; q++) p.partials[3 * blockIdx.x + q] = tot[q];
 }
 
 __global__ void __launch_bounds__(1024) k_edge_offsets_partials(EdgeOffsets p, int64_t n_tiles)
 {
-    // one block: exclusive scan of the per-tile triples, 1024 tiles at a time
-    __shared__ long long sm[3][33];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // one block, chunks of 4096 tiles: a thread loads four consecutive
+    // tiles' triples at once (twelve loads in flight), one block-wide scan
+    // of the thread sums per chunk
+    constexpr int kPer = 4;
     long long carry[3] = {0, 0, 0};
-    for (long long b = 0; b < n_tiles; b += 1024) {
-        const long long i = b + threadIdx.x;
-        for (int q = 0; q < 3; q++) {
-            const long long x = i < n_tiles ? p.partials[3 * i + q] : 0;
-            long long incl = x;
-            for (int o = 1; o < 32; o <<= 1) {
-                const long long y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
+    for (long long b = 0; b < n_tiles; b += 1024 * kPer) {
+        const long long i0 = b + (long long)threadIdx.x * kPer;
+        long long v[kPer][3], x[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < kPer; k++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                v[k][q] = i0 + k < n_tiles ? p.partials[3 * (i0 + k) + q] : 0;
+                x[q] += v[k][q];
             }
-            if (lane == 31) sm[q][warp] = incl;
-            __syncthreads();
-            if (warp == 0) {
-                const long long w = sm[q][lane];
-                long long wi = w;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const long long y = __shfl_up_sync(0xffffffffu, wi, o);
-                    if (lane >= o) wi += y;
-                }
-                sm[q][lane] = wi - w;
-                if (lane == 31) sm[q][32] = wi;
+        long long run[3], tot[3];
+        block_scan3<1024>(x, run, tot);
+#pragma unroll
+        for (int k = 0; k < kPer; k++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                if (i0 + k < n_tiles) p.partials[3 * (i0 + k) + q] = carry[q] + run[q];
+                run[q] += v[k][q];
             }
-            __syncthreads();
-            if (i < n_tiles) p.partials[3 * i + q] = carry[q] + sm[q][warp] + incl - x;
-            carry[q] += sm[q][32];
-            __syncthreads();
-        }
+#pragma unroll
+        for (int q = 0; q < 3; q++) carry[q] += tot[q];
     }
     if (threadIdx.x == 0) {
         if (p.et_off) p.et_off[p.E] = carry[0];
@@ -886,48 +894,38 @@ __global__ void __launch_bounds__(1024) k_edge_offsets_partials(EdgeOffsets p, i
     }
 }
 
-__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets p, const uint2 *erank)
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets p)
 {
-    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * 8;
-    long long x[3] = {0, 0, 0};
-    const uint32_t bits = slot_bits8(p, s0);
-    for (uint32_t m = bits; m; m &= m - 1) {
-        const int i = __ffs(m) - 1;
-        if (s0 + i >= p.n_slots) break;
-        int et, ef, ee;
-        slot_counts(p, s0 + i, et, ef, ee);
-        x[0] += et;
-        x[1] += ef;
-        x[2] += ee;
+    // the tile's edges are the ids [lo, hi): a run of consecutive ones a
+    // thread (at most kEdgeItems)
+    const long long t0 = (long long)blockIdx.x * kEdgeTile;
+    const int lo = rank_of(p.erank, t0);
+    const int hi = rank_of(p.erank, min(t0 + kEdgeTile, (long long)p.n_slots));
+    const int per = (hi - lo + kEdgeThreads - 1) / kEdgeThreads;
+    const int i0 = lo + per * (int)threadIdx.x;
+    const int k_end = min(per, hi - i0);
+    // per-edge lengths fit 8 + 8 + 16 bits: a thread's sums fit 32 bits
+    int x0 = 0, x1 = 0, x2 = 0;
+    for (int k = 0; k < k_end; k++) {
+        const uint32_t w = p.len[i0 + k];
+        x0 += w & 0xff;
+        x1 += (w >> 8) & 0xff;
+        x2 += w >> 16;
     }
-    long long excl[3], tot[3];
-    block_scan3(x, excl, tot);
+    long long x[3] = {x0, x1, x2}, excl[3], tot[3];
+    block_scan3<kEdgeThreads>(x, excl, tot);
     long long run[3];
     for (int q = 0; q < 3; q++) run[q] = p.partials[3 * blockIdx.x + q] + excl[q];
-    if (!bits) return;
-    int id = rank_of(erank, s0);
-    // the counts again (their loads hit the cache): registers for eight
-    // slots' counts would halve the blocks an SM holds
-    for (uint32_t m = bits; m; m &= m - 1) {
-        const int i = __ffs(m) - 1;
-        const long long s = s0 + i;
-        if (p.ev) {
-            const long long cell = s / 6;
-            const int j = (int)(s - 6 * cell);
-            const int4 w = __ldg(p.tvs + cell);
-            const int ia = j < 3 ? 0 : (j < 5 ? 1 : 2);
-            const int ib = j < 3 ? j + 1 : (j == 3 ? 2 : 3);
-            reinterpret_cast<int2 *>(p.ev)[id] = make_int2(get4(w, ia), get4(w, ib));
-        }
-        if (p.et_off) p.et_off[id] = run[0];
-        if (p.ef_off) p.ef_off[id] = run[1];
-        if (p.ee_off) p.ee_off[id] = run[2];
-        int et, ef, ee;
-        slot_counts(p, s, et, ef, ee);
-        run[0] += et;
-        run[1] += ef;
-        run[2] += ee;
-        id++;
+    // the words again (cache hits): keeping a run in registers would cost
+    // occupancy
+    for (int k = 0; k < k_end; k++) {
+        const uint32_t w = p.len[i0 + k];
+        if (p.et_off) p.et_off[i0 + k] = run[0];
+        if (p.ef_off) p.ef_off[i0 + k] = run[1];
+        if (p.ee_off) p.ee_off[i0 + k] = run[2];
+        run[0] += w & 0xff;
+        run[1] += (w >> 8) & 0xff;
+        run[2] += w >> 16;
     }
 }
 
@@ -1029,9 +1027,9 @@ void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int 
         off, V, window_count(n_entries, win_size), win_size, win);
 }
 
-size_t edge_offsets_scratch_bytes(int64_t n_slots)
+size_t edge_offsets_scratch_bytes(int64_t n_slots, int64_t E)
 {
-    return (size_t)(3 * (n_slots / kEdgeTile + 2)) * sizeof(int64_t);
+    return (size_t)(3 * (n_slots / kEdgeTile + 2)) * sizeof(int64_t) + (size_t)E * sizeof(uint32_t);
 }
 
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
@@ -1039,9 +1037,11 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
                          void *scratch, cudaStream_t s)
 {
-    EdgeOffsets p{eflag, reinterpret_cast<const unsigned short *>(ecnt), tvs, deg, n_slots,
-                  (int64_t *)scratch, et_off, ef_off, ee_off, ev, E};
     const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
+    int64_t *partials = (int64_t *)scratch;
+    uint32_t *len = reinterpret_cast<uint32_t *>(partials + 3 * (n_slots / kEdgeTile + 2));
+    EdgeOffsets p{eflag, reinterpret_cast<const unsigned short *>(ecnt), tvs, deg, erank, n_slots,
+                  partials, len, et_off, ef_off, ee_off, ev, E};
     if (tiles > 0) {
         Launch L("k_edge_offsets_reduce", s);
         k_edge_offsets_reduce<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p);
@@ -1052,7 +1052,7 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
     }
     if (tiles > 0) {
         Launch L("k_edge_offsets_down", s);
-        k_edge_offsets_down<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p, erank);
+        k_edge_offsets_down<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p);
     }
 }
 
