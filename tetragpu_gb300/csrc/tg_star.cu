@@ -689,8 +689,14 @@ __device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_
 // Sort every VT row ascending.  Rows starting in a window are staged in
 // shared memory and each entry lands at its rank in its row (cells in a row
 // are distinct); windows holding more than kCap entries fall back to an
-// insertion sort per row in global memory.
-__global__ void __launch_bounds__(kThreads)
+// insertion sort per row in global memory.  A block's time is mostly a chain
+// of dependent loads (window, offsets, cells, first cells): small blocks put
+// more chains in flight per SM.
+#ifndef TG_VTS_THREADS
+#define TG_VTS_THREADS 64
+#endif
+constexpr int kVtsThreads = TG_VTS_THREADS;
+__global__ void __launch_bounds__(kVtsThreads)
 k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt,
           const int4 *__restrict__ tvs, uint32_t *__restrict__ vflag, int64_t *__restrict__ vkey)
 {
@@ -1085,7 +1091,7 @@ void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int6
 {
     if (V == 0) return;
     Launch L("k_vt_sort", s);
-    k_vt_sort<<<n_windows(nvt), kThreads, 0, s>>>(vt_off, win, vt, tvs, vflag, vkey);
+    k_vt_sort<<<n_windows(nvt), kVtsThreads, 0, s>>>(vt_off, win, vt, tvs, vflag, vkey);
 }
 
 
