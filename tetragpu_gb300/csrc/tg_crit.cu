@@ -14,9 +14,9 @@
 //   k_crit_adj       field-independent: for every VV entry (v, u), the bitmask
 //                    of v's neighbours adjacent to u.  Thread per edge (both
 //                    of its entries), v's row staged in shared memory.
-//   k_crit_classify  field-dependent: lower/upper split, then a union-find
-//                    with path halving in shared memory over the adjacency
-//                    bits of same-kind neighbours; roots are counted.
+//   k_crit_classify  field-dependent: lower/upper split, then the components
+//                    of each kind counted by a bitmask search over the
+//                    adjacency masks of same-kind neighbours.
 #include "tg_internal.h"
 
 namespace tg {
@@ -140,18 +140,11 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
 
 constexpr int kClassifyThreads = 128;
 
-__device__ __forceinline__ int uf_find(unsigned char *p, int stride, int x)
-{
-    // path halving: every visited node skips to its grandparent
-    while (true) {
-        const int px = p[x * stride];
-        if (px == x) return x;
-        const int gx = p[px * stride];
-        p[x * stride] = (unsigned char)gx;
-        x = gx;
-    }
-}
-
+// Components of the lower and upper link subgraphs by bitmask search: a
+// component grows from its lowest unvisited member, each member reached
+// once adding its same-kind neighbours (its adjacency mask) to the frontier.
+// Every neighbour is visited exactly once, so a vertex costs deg iterations
+// whatever the link's shape (no data-dependent find loops).
 template <typename F>
 __global__ void __launch_bounds__(kClassifyThreads)
 k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
@@ -160,13 +153,10 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 {
     // rows [v0, v0 + nv); field and classes indexed from v0 (a vertex range
     // holds every neighbour of its vertices when it is a whole mesh of a batch)
-    __shared__ unsigned char parent_all[kMaxDeg * kClassifyThreads];
     const int64_t v = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= v0 + nv) return;
     const F *field = field_v0 - v0;
     unsigned *classes3 = classes3_v0 - 3 * v0;
-    unsigned char *parent = parent_all + threadIdx.x;  // parent[k * stride]
-    const int stride = kClassifyThreads;
     const int64_t b = vv_off[v];
     const int n = (int)(vv_off[v + 1] - b);
     unsigned lo = 0, up = 0;
@@ -178,26 +168,24 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
             const F fu = __ldg(field + u);
             const bool is_lower = (fu == fv) ? (u < (int)v) : (fu < fv);
             lower |= (unsigned long long)is_lower << k;
-            parent[k * stride] = (unsigned char)k;
         }
-        for (int k = 0; k < n; k++) {
-            const unsigned long long same = ((lower >> k) & 1ull) ? lower : ~lower;
-            // partners above k of the same kind
-            unsigned long long m = __ldg(adj + b + k) & same & (~0ull << k) & ~(1ull << k);
-            while (m) {
-                const int j = __ffsll((long long)m) - 1;
-                m &= m - 1;
-                const int ra = uf_find(parent, stride, k), rb = uf_find(parent, stride, j);
-                if (ra != rb) {
-                    if (ra < rb) parent[rb * stride] = (unsigned char)ra;
-                    else parent[ra * stride] = (unsigned char)rb;
-                }
+        const unsigned long long all = n == 64 ? ~0ull : (1ull << n) - 1ull;
+        unsigned long long rem = all;
+        while (rem) {
+            const int s = __ffsll((long long)rem) - 1;
+            const bool is_lo = (lower >> s) & 1ull;
+            const unsigned long long kind = is_lo ? lower : (all & ~lower);
+            unsigned long long comp = 1ull << s, frontier = comp;
+            while (frontier) {
+                const int j = __ffsll((long long)frontier) - 1;
+                frontier &= frontier - 1;
+                const unsigned long long nb = __ldg(adj + b + j) & kind & ~comp;
+                comp |= nb;
+                frontier |= nb;
             }
+            rem &= ~comp;
+            if (is_lo) lo++; else up++;
         }
-        for (int k = 0; k < n; k++)
-            if (parent[k * stride] == k) {
-                if ((lower >> k) & 1ull) lo++; else up++;
-            }
     }
     unsigned code;
     if (lo >= 1 && up == 0) code = 2;
