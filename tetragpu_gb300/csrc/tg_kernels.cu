@@ -48,45 +48,89 @@ __device__ __forceinline__ int pair_slot(int s, int t)
 // ---------------------------------------------------------------------------
 // k_canon
 // ---------------------------------------------------------------------------
+// A block's 1024 (cell, slot) pairs name far fewer distinct vertices on
+// meshes whose cells come in spatial order (a run of cubes shares its
+// corners): the block counts them in a shared-memory hash (vertex -> count;
+// each pair's place is its local rank there) and makes one global atomic per
+// distinct vertex, whose return value is the block's base in that vertex's
+// VT row.
+constexpr int kCanonHash = 2048;   // twice the block's pairs: never full
+
 __global__ void __launch_bounds__(256)
 k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, int4 *occ, DevStatus *st,
         int aligned)
 {
+    __shared__ int hkey[kCanonHash], hcnt[kCanonHash];
+    for (int i = threadIdx.x; i < kCanonHash; i += blockDim.x) {
+        hkey[i] = -1;
+        hcnt[i] = 0;
+    }
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= T) return;
-    int a, b, d, e;
-    if (aligned) {
-        int4 w = reinterpret_cast<const int4 *>(tv)[c];
-        a = w.x; b = w.y; d = w.z; e = w.w;
-    } else {
-        a = tv[4 * c]; b = tv[4 * c + 1]; d = tv[4 * c + 2]; e = tv[4 * c + 3];
+    int q[4];
+    bool ok = false;
+    if (c < T) {
+        int a, b, d, e;
+        if (aligned) {
+            int4 w = reinterpret_cast<const int4 *>(tv)[c];
+            a = w.x; b = w.y; d = w.z; e = w.w;
+        } else {
+            a = tv[4 * c]; b = tv[4 * c + 1]; d = tv[4 * c + 2]; e = tv[4 * c + 3];
+        }
+        // A rejected cell is overwritten with -1s (the input may alias tvs)
+        // and takes no part in the counts; every later kernel skips it, and
+        // the host reports the error before anything reads the mesh again.
+        if ((unsigned)a >= (unsigned)V || (unsigned)b >= (unsigned)V ||
+            (unsigned)d >= (unsigned)V || (unsigned)e >= (unsigned)V) {
+            atomicOr(&st->flags, ST_BAD_ID);
+            atomicMin(&st->bad_cell, (int)c);
+            tvs[c] = make_int4(-1, -1, -1, -1);
+        } else {
+            TG_CSWAP(a, b);
+            TG_CSWAP(d, e);
+            TG_CSWAP(a, d);
+            TG_CSWAP(b, e);
+            TG_CSWAP(b, d);
+            if (a == b || b == d || d == e) {
+                atomicOr(&st->flags, ST_DUP_VERTEX);
+                atomicMin(&st->bad_cell, (int)c);
+                tvs[c] = make_int4(-1, -1, -1, -1);
+            } else {
+                tvs[c] = make_int4(a, b, d, e);
+                q[0] = a; q[1] = b; q[2] = d; q[3] = e;
+                ok = true;
+            }
+        }
     }
-    // A rejected cell is overwritten with -1s (the input may alias tvs) and
-    // takes no part in the counts; every later kernel skips it, and the host
-    // reports the error before anything reads the mesh again.
-    if ((unsigned)a >= (unsigned)V || (unsigned)b >= (unsigned)V ||
-        (unsigned)d >= (unsigned)V || (unsigned)e >= (unsigned)V) {
-        atomicOr(&st->flags, ST_BAD_ID);
-        atomicMin(&st->bad_cell, (int)c);
-        tvs[c] = make_int4(-1, -1, -1, -1);
-        return;
+    __syncthreads();
+    int hs[4], rk[4];
+    if (ok) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            unsigned h = ((unsigned)q[k] * 0x9E3779B1u) >> 21;   // 11 bits
+            hs[k] = 0;
+            rk[k] = 0;
+            for (int probe = 0; probe < kCanonHash; probe++) {
+                const int old = atomicCAS(&hkey[h], -1, q[k]);
+                if (old == -1 || old == q[k]) {
+                    hs[k] = (int)h;
+                    rk[k] = atomicAdd(&hcnt[h], 1);
+                    break;
+                }
+                h = (h + 1) & (kCanonHash - 1);
+            }
+        }
     }
-    TG_CSWAP(a, b);
-    TG_CSWAP(d, e);
-    TG_CSWAP(a, d);
-    TG_CSWAP(b, e);
-    TG_CSWAP(b, d);
-    if (a == b || b == d || d == e) {
-        atomicOr(&st->flags, ST_DUP_VERTEX);
-        atomicMin(&st->bad_cell, (int)c);
-        tvs[c] = make_int4(-1, -1, -1, -1);
-        return;
+    __syncthreads();
+    // the count so far is the block's place in each vertex's VT row (rows
+    // are sorted afterwards)
+    for (int i = threadIdx.x; i < kCanonHash; i += blockDim.x) {
+        const int n = hcnt[i];
+        if (n) hcnt[i] = atomicAdd(deg_t + hkey[i], n);
     }
-    tvs[c] = make_int4(a, b, d, e);
-    // the count so far is the cell's place in each vertex's VT row (rows are
-    // sorted afterwards)
-    occ[c] = make_int4(atomicAdd(deg_t + a, 1), atomicAdd(deg_t + b, 1), atomicAdd(deg_t + d, 1),
-                       atomicAdd(deg_t + e, 1));
+    __syncthreads();
+    if (ok)
+        occ[c] = make_int4(hcnt[hs[0]] + rk[0], hcnt[hs[1]] + rk[1], hcnt[hs[2]] + rk[2],
+                           hcnt[hs[3]] + rk[3]);
 }
 
 // ---------------------------------------------------------------------------
