@@ -45,6 +45,14 @@ __device__ __forceinline__ int pair_slot(int s, int t)
 #define TG_CSWAP(x, y) \
     if ((x) > (y)) { int _t = (x); (x) = (y); (y) = _t; }
 
+// one comparator of a sorting network: (x, y) <- (min, max)
+__device__ __forceinline__ void cswap(int &x, int &y)
+{
+    const int lo = min(x, y);
+    y = max(x, y);
+    x = lo;
+}
+
 // ---------------------------------------------------------------------------
 // k_canon
 // ---------------------------------------------------------------------------
@@ -213,19 +221,23 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__re
             fe[3LL * f + 2] = row[pair_slot(sl[1], sl[2])];
         }
         const int o = (cells.x == (int)c) ? cells.y : cells.x;
-        if (o >= 0) nbr[n++] = o;
+        nbr[col] = o >= 0 ? o : INT_MAX;   // no cell across a boundary face
+        n += o >= 0;
     }
     if (tt) {
-        for (int i = 1; i < n; i++) {
-            const int x = nbr[i];
-            int j = i - 1;
-            while (j >= 0 && nbr[j] > x) { nbr[j + 1] = nbr[j]; j--; }
-            nbr[j + 1] = x;
-        }
+        // a sorting network (no data-dependent loops); the missing
+        // neighbours sort last
+        cswap(nbr[0], nbr[1]);
+        cswap(nbr[2], nbr[3]);
+        cswap(nbr[0], nbr[2]);
+        cswap(nbr[1], nbr[3]);
+        cswap(nbr[1], nbr[2]);
         const int64_t off = 4 * c - rank_of(brank, 4 * c);
         tt_off[c] = off;
         int *row = tt + off;
-        for (int i = 0; i < n; i++) row[i] = nbr[i];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            if (i < n) row[i] = nbr[i];
     }
 }
 
@@ -235,27 +247,28 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
 {
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
+    // the faces of the face's two cells, f itself (once in each row) and a
+    // missing second cell as INT_MAX, sorted by a 19-comparator network: the
+    // first 6 (interior) or 3 (boundary) are the row
     const int2 cells = reinterpret_cast<const int2 *>(ft)[f];
-    int r[6];
-    int n = 0;
-    for (int s = 0; s < 2; s++) {
-        const int c = s ? cells.y : cells.x;
-        if (c < 0) continue;
-        const int4 w = reinterpret_cast<const int4 *>(tf)[c];
+    const int4 w0 = reinterpret_cast<const int4 *>(tf)[cells.x];
+    const int4 w1 = cells.y >= 0 ? reinterpret_cast<const int4 *>(tf)[cells.y]
+                                 : make_int4((int)f, (int)f, (int)f, (int)f);
+    int r[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int g = get4(w, k);
-            if (g != (int)f) r[n++] = g;
-        }
-    }
-    for (int i = 1; i < n; i++) {
-        const int x = r[i];
-        int j = i - 1;
-        while (j >= 0 && r[j] > x) { r[j + 1] = r[j]; j--; }
-        r[j + 1] = x;
-    }
+    for (int k = 0; k < 8; k++)
+        if (r[k] == (int)f) r[k] = INT_MAX;
+    cswap(r[0], r[2]); cswap(r[1], r[3]); cswap(r[4], r[6]); cswap(r[5], r[7]);
+    cswap(r[0], r[4]); cswap(r[1], r[5]); cswap(r[2], r[6]); cswap(r[3], r[7]);
+    cswap(r[0], r[1]); cswap(r[2], r[3]); cswap(r[4], r[5]); cswap(r[6], r[7]);
+    cswap(r[2], r[4]); cswap(r[3], r[5]);
+    cswap(r[1], r[4]); cswap(r[3], r[6]);
+    cswap(r[1], r[2]); cswap(r[3], r[4]); cswap(r[5], r[6]);
+    const int n = cells.y >= 0 ? 6 : 3;
     int *row = ff + ff_off[f];
-    for (int i = 0; i < n; i++) row[i] = r[i];
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+        if (i < n) row[i] = r[i];
 }
 
 // EE: a warp takes 32 consecutive edges (each lane fetches one edge's
