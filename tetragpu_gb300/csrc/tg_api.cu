@@ -354,7 +354,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
     Temps tmp(s);
 
     if (want_star) {
-        TRY(reset_status(m, s));
+        // the status is clean: the read-back that ended the last call reset it
         // ---- pass A: first occurrences, neighbour counts, ET/EF row lengths ----
         const int64_t nwe = (6 * T + 31) / 32, nwf = (4 * T + 31) / 32;
         uint32_t *eflag, *fflag, *fbnd;
@@ -555,7 +555,6 @@ tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const voi
     const int64_t V = m->V;
     const Rel &vv = m->rel[TG_REL_VV];
     if (!m->cadj) {
-        TRY(reset_status(m, s));
         TRY(dalloc(&m->cadj, vv.entries, s));
         int32_t *vv_win;
         TRY(dalloc(&vv_win, window_count(vv.entries, crit_window()) + 1, s));
@@ -680,9 +679,9 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
         TRY(dalloc(&m->vtp, 4 * T, s));
         launch_vtp_fill(m->vorder, m->pofs, V, vt_off, vt, m->vtp, s);
         TRY(dalloc(&m->st_win, window_count(4 * T, star_window()) + 1, s));
-        launch_window_starts(m->pofs, V, 4 * T, star_window(), m->st_win, s);
         TRY(dalloc(&m->st_win_b, window_count(4 * T, star_window_b()) + 1, s));
-        launch_window_starts(m->pofs, V, 4 * T, star_window_b(), m->st_win_b, s);
+        launch_window_starts(m->pofs, V, 4 * T, star_window(), m->st_win, s, star_window_b(),
+                             m->st_win_b);
     }
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);

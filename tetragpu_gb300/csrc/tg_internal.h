@@ -64,7 +64,7 @@ void launch_reset_status(DevStatus *st, cudaStream_t s);
 // Status word and up to 8 sizes (int64, or int32 sign-extended) stored by a
 // kernel into device-mapped pinned host memory (no copy engine involved)
 struct PublishArgs {
-    const DevStatus *st;
+    DevStatus *st;           // reset once copied
     const void *src[8];
     int wide[8];
     int n;
@@ -86,7 +86,8 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
 // after entry win_size * w (w = 0 .. window_count), win[window_count] = rows.
 int64_t window_count(int64_t n_entries, int win_size);
 void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int win_size,
-                          int32_t *win, cudaStream_t s);
+                          int32_t *win, cudaStream_t s, int win_size2 = 0,
+                          int32_t *win2 = nullptr);
 int star_window();    // the window size of star pass A over VT
 int star_window_b();  // the window size of star pass B
 // sort every VT row (tg_star.cu): window-staged, coalesced.  Also marks each

@@ -543,6 +543,8 @@ void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int w
                                                             reinterpret_cast<long long *>(out), counts);
 }
 
+// copies the status and the sizes to mapped host memory, then resets the
+// status for the next call on the mesh (the host has consumed it)
 __global__ void k_publish(PublishArgs a)
 {
     if (threadIdx.x != 0) return;
@@ -550,6 +552,11 @@ __global__ void k_publish(PublishArgs a)
     for (int i = 0; i < a.n; i++)
         a.h_sz[i] = a.wide[i] ? *(const int64_t *)a.src[i] : (int64_t) * (const int32_t *)a.src[i];
     __threadfence_system();
+    a.st->flags = 0;
+    a.st->bad_cell = INT_MAX;
+    a.st->bad_vertex = INT_MAX;
+    a.st->max_star = 0;
+    a.st->max_deg = 0;
 }
 
 void launch_publish(const PublishArgs &a, cudaStream_t s)

@@ -937,18 +937,27 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets 
 
 // win[w] = first vertex whose row starts at or after entry kWin * w, for
 // w in [0, n_win], with win[n_win] = V.  Vertex v owns the windows w with
-// off[v-1] < kWin * w <= off[v].
+// off[v-1] < kWin * w <= off[v].  A second table over the same offsets with
+// another window size (win2, or null) comes from the same launch.
+__device__ __forceinline__ void window_owner(const long long lo, const long long hi, int64_t v,
+                                             int64_t n_win, int win_size, int *win)
+{
+    long long w = lo < 0 ? 0 : lo / win_size + 1;
+    const long long w_hi = hi / win_size;
+    for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
+}
+
 __global__ void __launch_bounds__(256)
 k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int win_size,
-                int *__restrict__ win)
+                int *__restrict__ win, int64_t n_win2, int win_size2, int *__restrict__ win2)
 {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v > V) return;
     const long long lo = v == 0 ? -1 : off[v - 1];
-    const long long hi = v == V ? (long long)win_size * n_win : off[v];
-    long long w = lo < 0 ? 0 : lo / win_size + 1;
-    const long long w_hi = hi / win_size;
-    for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
+    window_owner(lo, v == V ? (long long)win_size * n_win : off[v], v, n_win, win_size, win);
+    if (win2)
+        window_owner(lo, v == V ? (long long)win_size2 * n_win2 : off[v], v, n_win2, win_size2,
+                     win2);
 }
 
 // ---------------------------------------------------------------------------
@@ -1026,11 +1035,12 @@ int star_window_b() { return kWinB; }
 int64_t window_count(int64_t n_entries, int win_size) { return n_entries / win_size + 1; }
 
 void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int win_size,
-                          int32_t *win, cudaStream_t s)
+                          int32_t *win, cudaStream_t s, int win_size2, int32_t *win2)
 {
     Launch L("k_window_starts", s);
     k_window_starts<<<(unsigned)((V + 1 + 255) / 256), 256, 0, s>>>(
-        off, V, window_count(n_entries, win_size), win_size, win);
+        off, V, window_count(n_entries, win_size), win_size, win,
+        win2 ? window_count(n_entries, win_size2) : 0, win_size2, win2);
 }
 
 size_t edge_offsets_scratch_bytes(int64_t n_slots, int64_t E)
