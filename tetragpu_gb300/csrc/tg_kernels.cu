@@ -320,18 +320,12 @@ __device__ __forceinline__ void ee_merge_one(const int *__restrict__ eid, int64_
             x[r] = upper ? max(x[r], y) : min(x[r], y);
         }
     }
-    // the first copy of e
-    int pe = N;
-#pragma unroll
-    for (int r = R - 1; r >= 0; r--) {
-        const unsigned m = __ballot_sync(kFull, x[r] == ei);
-        if (m) pe = 32 * r + __ffs(m) - 1;
-    }
+    // the row is sorted: an entry above e follows both copies of e
     const int n = na + nb;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int p = lane + 32 * r;
-        if (p < n && x[r] != ei) out[p - (p > pe ? 2 : 0)] = x[r];
+        if (p < n && x[r] != ei) out[p - (x[r] > ei ? 2 : 0)] = x[r];
     }
 }
 
@@ -349,7 +343,7 @@ static_assert(kEeGroup == 4 || kEeGroup == 8, "lanes per edge: 4 or 8");
 template <int G>
 __device__ __forceinline__ void ee_merge_group(const int *__restrict__ eid, int64_t ra, int na,
                                                int64_t rb, int nb, int ei, int *__restrict__ out,
-                                               int gl, int g)
+                                               int gl)
 {
     constexpr int R = 32 / G;
     int x[R];
@@ -384,17 +378,12 @@ __device__ __forceinline__ void ee_merge_group(const int *__restrict__ eid, int6
             x[r] = upper ? max(x[r], y) : min(x[r], y);
         }
     }
-    int pe = 32;
-#pragma unroll
-    for (int r = R - 1; r >= 0; r--) {
-        const unsigned m = (__ballot_sync(kFull, x[r] == ei) >> (G * g)) & ((1u << G) - 1u);
-        if (m) pe = G * r + __ffs(m) - 1;
-    }
+    // the row is sorted: an entry above e follows both copies of e
     const int n = na + nb;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int p = gl + G * r;
-        if (p < n && x[r] != ei) out[p - (p > pe ? 2 : 0)] = x[r];
+        if (p < n && x[r] != ei) out[p - (x[r] > ei ? 2 : 0)] = x[r];
     }
 }
 
@@ -429,7 +418,7 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
         int na = __shfl_sync(kFull, my_na, src), nb = __shfl_sync(kFull, my_nb, src);
         const int64_t o = __shfl_sync(kFull, my_out, src);
         if (which >= n_small) na = nb = 0;  // an idle group: nothing to write
-        ee_merge_group<G>(eid, ra, na, rb, nb, (int)(e0 + src), ee + o, gl, g);
+        ee_merge_group<G>(eid, ra, na, rb, nb, (int)(e0 + src), ee + o, gl);
     }
     // longer rows one edge at a time over the whole warp
     for (unsigned rest = big; rest; rest &= rest - 1) {
