@@ -95,34 +95,49 @@ __device__ __forceinline__ int rank_of(const uint2 *__restrict__ rk, long long p
     const uint2 w = __ldg(rk + (p >> 5));
     return (int)w.y + __popc(w.x & ((1u << (p & 31)) - 1u));
 }
-__device__ __forceinline__ int ctz64(unsigned long long m) { return __ffsll((long long)m) - 1; }
+// Star-position masks: bit j = position j of a vertex's star.  A block
+// whose window holds only stars of at most 32 cells works with 32-bit masks
+// (the GPU's integer operations are 32-bit: a 64-bit and, shift or
+// find-first-set costs several instructions), any other with 64-bit ones
+// (stars of at most kMaxStar = 64 cells).  Both run the same templated code;
+// the masks in global memory are 64-bit either way.
+__device__ __forceinline__ int mctz(unsigned m) { return __ffs((int)m) - 1; }
+__device__ __forceinline__ int mctz(unsigned long long m) { return __ffsll((long long)m) - 1; }
+__device__ __forceinline__ int mpopc(unsigned m) { return __popc(m); }
+__device__ __forceinline__ int mpopc(unsigned long long m) { return __popcll(m); }
+constexpr int kNarrowStar = 32;   // the most cells a star may have for 32-bit masks
 
-struct Stage {
+// Pass A's shared memory: the fields that do not depend on the mask width
+// first (staged before the width is chosen), the masks last.
+struct StageBaseA {
     int cell[kCap];
     int4 tv[kCap];
     int vid[kCap];
     int meta[kCap];                     // row start | D << 10 | slot of v << 20
     unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
-    unsigned long long hmask[kHash];    // star positions whose cell holds the neighbour
     short cslot[kCap][4];               // hash slot of each entry's 3 candidates (other vertices)
     int cnt[kCap];                      // per row start: neighbours counted / listed so far
-    int n, vlo, vhi, full;
+    int n, vlo, vhi, full, wide;
     long long base;
+};
+template <typename M>
+struct Stage : StageBaseA {
+    M hmask[kHash];                     // star positions whose cell holds the neighbour
 };
 
 // static shared memory is capped at 48 KiB per block
-static_assert(sizeof(Stage) <= 48 * 1024, "star stage exceeds the static shared-memory limit");
+static_assert(sizeof(Stage<unsigned long long>) <= 48 * 1024,
+              "star stage exceeds the static shared-memory limit");
 
 // Pass B stages the same window without a hash: pass A leaves every VT
 // entry's three candidate masks in global memory.  It also lists each
 // vertex's neighbours (at 3 * row start, the most a row of D cells can have
 // is 3D) with their edge ids.
-struct StageM {
+struct StageBaseB {
     int cell[kCapB];
     int4 tv[kCapB];
     int vid[kCapB];
     int meta[kCapB];                     // row start | D << 10 | slot of v << 20
-    unsigned long long cm[kCapB][3];     // star positions holding each candidate
     int hv[kCapB][3];                    // at first sightings: list index, then edge id
     int cnt[kCapB];
     int list_u[3 * kCapB];               // neighbours, then (after pass 2) their edge ids
@@ -130,10 +145,15 @@ struct StageM {
                                         // candidate): n_owned
                                         // owned ones (u > v) from the front, n_work others
                                         // from the back
-    int n, vlo, vhi, n_work, n_owned;
+    int n, vlo, vhi, n_work, n_owned, wide;
     long long base;
 };
-static_assert(sizeof(StageM) <= 48 * 1024, "star stage B exceeds the static shared-memory limit");
+template <typename M>
+struct StageM : StageBaseB {
+    M cm[kCapB][3];                      // star positions holding each candidate
+};
+static_assert(sizeof(StageM<unsigned long long>) <= 48 * 1024,
+              "star stage B exceeds the static shared-memory limit");
 
 __device__ __forceinline__ int m_rs(int m) { return m & 1023; }
 __device__ __forceinline__ int m_D(int m) { return (m >> 10) & 1023; }
@@ -144,7 +164,8 @@ __device__ __forceinline__ unsigned hslot(unsigned long long key)
     return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - kHashBits));
 }
 
-__device__ __forceinline__ int h_insert(Stage &S, unsigned long long key, unsigned long long bits)
+template <typename M>
+__device__ __forceinline__ int h_insert(Stage<M> &S, unsigned long long key, M bits)
 {
     unsigned h = hslot(key);
     for (int probe = 0; probe < kHash; probe++) {
@@ -163,13 +184,13 @@ __device__ __forceinline__ unsigned long long hk(int rs, int u)
     return ((unsigned long long)(unsigned)rs << 32) | (unsigned)u;
 }
 
-// Stage the block's window and fill the (vertex, neighbour) table.  Returns
-// false (block-uniformly) when the window cannot be handled here.  win[b] is
-// the first vertex whose row starts at or after entry kWin * b.
-__device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
-                               const int *__restrict__ win, const int *__restrict__ vorder,
-                               const int *__restrict__ vtp, const int4 *__restrict__ tvs,
-                               DevStatus *st)
+// Stage the block's window: its bounds, every row's metadata (and whether a
+// star has more than kNarrowStar cells), empty hash keys.  Returns false
+// (block-uniformly) when the window cannot be handled here.  win[b] is the
+// first vertex whose row starts at or after entry kWin * b.
+__device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
+                           const int *__restrict__ win, const int *__restrict__ vorder,
+                           DevStatus *st)
 {
     if (threadIdx.x == 0) {
         const int plo = win[blockIdx.x], phi = win[blockIdx.x + 1];
@@ -178,14 +199,11 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
         S.base = pofs[plo];
         S.n = (int)(pofs[phi] - S.base);
         S.full = 0;
+        S.wide = 0;
     }
-    for (int h = threadIdx.x; h < kHash; h += blockDim.x) {
-        S.hkey[h] = kEmpty;
-        S.hmask[h] = 0ull;
-    }
+    for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hkey[h] = kEmpty;
     __syncthreads();
-    const int n = S.n;
-    if (n > kCap) {
+    if (S.n > kCap) {
         if (threadIdx.x == 0) {
             atomicOr(&st->flags, ST_HEAVY_STAR);
             atomicMin(&st->bad_vertex, vorder[S.vlo]);
@@ -203,19 +221,33 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
             atomicMin(&st->bad_vertex, v);
             S.full = 1;
         }
+        if (D > kNarrowStar) S.wide = 1;
         for (int j = 0; j < D; j++) {
             S.vid[rs + j] = v;
             S.meta[rs + j] = rs | (D << 10);
         }
         S.cnt[rs] = 0;
     }
+    __syncthreads();
+    return !S.full;
+}
+
+// Stage the window's cells and fill the (vertex, neighbour) table.  Returns
+// false (block-uniformly) when the table overflows.
+template <typename M>
+__device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vtp,
+                                     const int4 *__restrict__ tvs, const int *__restrict__ vorder,
+                                     DevStatus *st)
+{
+    for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hmask[h] = 0;
+    const int n = S.n;
+    const long long base = S.base;
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int c = __ldg(vtp + base + e);
         S.cell[e] = c;
         S.tv[e] = __ldg(tvs + c);
     }
     __syncthreads();
-    if (S.full) return false;
     // insert the 3 other vertices of every staged cell, keyed by the row
     for (int e0 = 0; e0 < n; e0 += blockDim.x) {
         const int e = e0 + threadIdx.x;
@@ -243,8 +275,9 @@ __device__ bool stage_and_hash(Stage &S, const int64_t *__restrict__ pofs,
             const int leader = __ffs(grp) - 1;
             int h = 0;
             if ((int)(threadIdx.x & 31) == leader) {
-                const unsigned long long bits =
-                    shift >= 0 ? (unsigned long long)grp << shift : (unsigned long long)grp >> -shift;
+                // the group's row positions (below the star's size, so
+                // within the mask's width)
+                const M bits = shift >= 0 ? (M)grp << shift : (M)grp >> -shift;
                 h = h_insert(S, key, bits);
                 if (h < 0) {
                     S.full = 1;
@@ -286,15 +319,14 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
+template <typename M>
+__device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_work)
 {
-    __shared__ Stage S;
-    __shared__ int n_work;
     // first sightings of owned edges (entry << 2 | candidate), in the hash
     // keys' space: after the table is built only its masks are read
     static_assert(sizeof(S.hkey) >= 3 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
-    if (!stage_and_hash(S, a.pofs, a.win, a.vorder, a.vtp, a.tvs, a.st)) return;
+    if (!stage_cells_and_hash(S, a.vtp, a.tvs, a.vorder, a.st)) return;
     const int n = S.n;
     if (threadIdx.x == 0) n_work = 0;
     __syncthreads();
@@ -303,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
         const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
         const int4 w = S.tv[e];
         const int c = S.cell[e];
-        unsigned long long cm[3];
+        M cm[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             cm[k] = S.hmask[S.cslot[e][k]];
@@ -311,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            if (ctz64(cm[k]) != pos) continue;                  // not the first sighting
+            if (mctz(cm[k]) != pos) continue;                  // not the first sighting
             atomicAdd(&S.cnt[rs], 1);
             if (get4(w, k + (k >= sv)) > v) work[atomicAdd(&n_work, 1)] = (e << 2) | k;
         }
@@ -322,11 +354,11 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
             const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
             for (int o = o_lo; o <= o_hi; o++) {
                 const int ko = cand_of(o, sv);      // the omitted candidate
-                const unsigned long long mf = ko == 0 ? cm[1] & cm[2] : (ko == 1 ? cm[0] & cm[2] : cm[0] & cm[1]);
-                if (ctz64(mf) != pos) continue;
+                const M mf = ko == 0 ? cm[1] & cm[2] : (ko == 1 ? cm[0] & cm[2] : cm[0] & cm[1]);
+                if (mctz(mf) != pos) continue;
                 const long long q = 4LL * c + (3 - o);
                 set_bit(a.fflag, q);
-                const int ncell = __popcll(mf);
+                const int ncell = mpopc(mf);
                 if (ncell == 1) set_bit(a.fbnd, q);
                 if (ncell > 2) {
                     atomicOr(&a.st->flags, ST_NONMANIFOLD_FACE);
@@ -346,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
     for (int tt = threadIdx.x; tt < span; tt += blockDim.x) {   // block-uniform trip count
         const int i = tt / L, sub = tt % L;
         int n_ef = 0;
-        unsigned long long mu = 0;
+        M mu = 0;
         long long p = 0;
         if (i < nw) {
             const int e = work[i] >> 2, k = work[i] & 3;
@@ -356,16 +388,16 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
             const int u = get4(S.tv[e], t);
             mu = S.hmask[S.cslot[e][k]];
             p = 6LL * S.cell[e] + pair_slot(sv, t);
-            unsigned long long mm = mu;
+            M mm = mu;
             for (int q = 0; q < sub; q++) mm &= mm - 1;
             while (mm) {
-                const int j = ctz64(mm);
+                const int j = mctz(mm);
                 const int ej = rs + j;
                 const int ku = cand_of(slot_of(S.tv[ej], u), m_sv(S.meta[ej]));
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++) {
                     if (kk == ku) continue;
-                    n_ef += ctz64(mu & S.hmask[S.cslot[ej][kk]]) == j;
+                    n_ef += mctz(mu & S.hmask[S.cslot[ej][kk]]) == j;
                 }
 #pragma unroll
                 for (int q = 0; q < L; q++) mm &= mm - 1;
@@ -375,7 +407,7 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
         for (int off = 1; off < L; off <<= 1) n_ef += __shfl_xor_sync(0xffffffffu, n_ef, off);
         if (i < nw && sub == 0) {
             set_bit(a.eflag, p);
-            a.ecnt[p] = (unsigned short)(__popcll(mu) | (n_ef << 8));
+            a.ecnt[p] = (unsigned short)(mpopc(mu) | (n_ef << 8));
         }
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -390,11 +422,24 @@ __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
     }
 }
 
+__global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
+{
+    __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
+    __shared__ int n_work;
+    StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
+    if (!stage_rows(S, a.pofs, a.win, a.vorder, a.st)) return;
+    if (S.wide)   // block-uniform
+        star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, n_work);
+    else
+        star_a_body(*reinterpret_cast<Stage<unsigned> *>(raw), a, n_work);
+}
+
 // ---------------------------------------------------------------------------
-// Stage pass B's window: rows, cells, cell vertices and the candidate
-// masks pass A computed.  Pass A has already rejected every window this
-// cannot hold, so nothing here fails.
-__device__ void stage_masks(StageM &S, const StarB &b)
+// Stage pass B's window: rows (and whether a star has more than kNarrowStar
+// cells), then cells, cell vertices and the candidate masks pass A computed.
+// Pass A has already rejected every window this cannot hold, so nothing here
+// fails.
+__device__ void stage_rows_b(StageBaseB &S, const StarB &b)
 {
     if (threadIdx.x == 0) {
         const int plo = b.win[blockIdx.x], phi = b.win[blockIdx.x + 1];
@@ -404,43 +449,53 @@ __device__ void stage_masks(StageM &S, const StarB &b)
         S.n = (int)(b.pofs[phi] - S.base);
         S.n_work = 0;
         S.n_owned = 0;
+        S.wide = 0;
     }
     __syncthreads();
-    const int n = S.n;
     const long long base = S.base;
     for (int i = S.vlo + threadIdx.x; i < S.vhi; i += blockDim.x) {
         const int rs = (int)(b.pofs[i] - base);
         const int D = (int)(b.pofs[i + 1] - b.pofs[i]);
         if (D == 0) continue;
         const int v = b.vorder[i];
+        if (D > kNarrowStar) S.wide = 1;
         for (int j = 0; j < D; j++) {
             S.vid[rs + j] = v;
             S.meta[rs + j] = rs | (D << 10);
         }
         S.cnt[rs] = 0;
     }
+    __syncthreads();
+}
+
+template <typename M>
+__device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b)
+{
+    const int n = S.n;
+    const long long base = S.base;
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int c = __ldg(b.vtp + base + e);
         S.cell[e] = c;
         S.tv[e] = __ldg(b.tvs + c);
 #pragma unroll
-        for (int k = 0; k < 3; k++) S.cm[e][k] = __ldg(b.emask + k * b.nvt + base + e);
+        for (int k = 0; k < 3; k++) S.cm[e][k] = (M)__ldg(b.emask + k * b.nvt + base + e);
     }
     __syncthreads();
 }
 
 // hv entry of candidate u of entry e: the one at u's first sighting in e's row
-__device__ __forceinline__ int hv_of(const StageM &S, int e, int k, int rs, int u)
+template <typename M>
+__device__ __forceinline__ int hv_of(const StageM<M> &S, int e, int k, int rs, int u)
 {
-    const int f = rs + ctz64(S.cm[e][k]);
+    const int f = rs + mctz(S.cm[e][k]);
     if (f == e) return S.hv[e][k];
     return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
 }
 
-__global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
+template <typename M>
+__device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
 {
-    __shared__ StageM S;
-    stage_masks(S, b);
+    stage_cells_b(S, b);
     const int n = S.n;
 
     // 1. list every vertex's neighbours (each at its first sighting); the
@@ -454,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
         S.meta[e] = m | (sv << 20);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            if (ctz64(S.cm[e][k]) != pos) continue;
+            if (mctz(S.cm[e][k]) != pos) continue;
             const int u = get4(w, k + (k >= sv));
             const int li = atomicAdd(&S.cnt[rs], 1);
             S.list_u[3 * rs + li] = u;
@@ -511,7 +566,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
             const int i = t / L, sub = t % L;
             const bool act = i < n_owned;
             int rs = 0, u = 0, id = 0;
-            unsigned long long mu = 0;
+            M mu = 0;
             if (act) {
                 const int e = (S.work[i] >> 2) & 511, k = S.work[i] & 3;
                 const int m = S.meta[e];
@@ -520,16 +575,16 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
                 mu = S.cm[e][k];
                 id = S.hv[e][k];
             }
-            const int rounds = (__popcll(mu) + L - 1) / L;
+            const int rounds = (mpopc(mu) + L - 1) / L;
             const int max_rounds = __reduce_max_sync(0xffffffffu, rounds);
             long long et_p = act && b.et ? b.et_off[id] : 0;
             long long ef_p = act && b.ef ? b.ef_off[id] : 0;
-            unsigned long long rest = mu;
+            M rest = mu;
             for (int r = 0; r < max_rounds; r++) {
                 // this lane's cell: the sub-th lowest remaining bit
-                unsigned long long mine = rest;
+                M mine = rest;
                 for (int q = 0; q < sub; q++) mine &= mine - 1;
-                const int j = mine ? ctz64(mine) : -1;
+                const int j = mine ? mctz(mine) : -1;
                 int nf = 0, col0 = 0, col1 = 0;
                 long long q0 = 0;
                 if (j >= 0) {
@@ -542,7 +597,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++) {
                         if (kk == ku) continue;
-                        if (ctz64(mu & S.cm[ej][kk]) != j) continue;
+                        if (mctz(mu & S.cm[ej][kk]) != j) continue;
                         const int tx = kk + (kk >= sj);
                         const int c = 3 - (6 - sj - su - tx);   // the omitted slot is the fourth
                         if (nf == 0) col0 = c; else col1 = c;
@@ -599,16 +654,16 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
                 for (int o = o_lo; o <= o_hi; o++) {
                     const int ko = cand_of(o, sv);
                     const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
-                    const unsigned long long mf = S.cm[e][ka] & S.cm[e][kb];
-                    if (ctz64(mf) != pos) continue;
+                    const M mf = S.cm[e][ka] & S.cm[e][kb];
+                    if (mctz(mf) != pos) continue;
                     const int fid = rank_of(b.frank, 4LL * c + (3 - o));
                     if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                    const unsigned long long m2 = mf & (mf - 1);
+                    const M m2 = mf & (mf - 1);
                     if (!m2) {
                         if (b.ft) b.ft[2LL * fid + 1] = -1;
                         continue;
                     }
-                    const int j2 = rs + ctz64(m2);
+                    const int j2 = rs + mctz(m2);
                     const int c2 = S.cell[j2];
                     if (b.ft) b.ft[2LL * fid + 1] = c2;
                     if (b.tf) {
@@ -630,6 +685,17 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
             b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
         }
     }
+}
+
+__global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
+{
+    __shared__ __align__(16) unsigned char raw[sizeof(StageM<unsigned long long>)];
+    StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
+    stage_rows_b(S, b);
+    if (S.wide)   // block-uniform
+        star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b);
+    else
+        star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b);
 }
 
 // The faces in id order, one thread per cell: the cell's first-occurrence
