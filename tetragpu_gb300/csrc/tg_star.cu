@@ -298,7 +298,10 @@ __device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vtp,
     return true;
 }
 
-__device__ __forceinline__ void set_bit(uint32_t *bits, long long p)
+// Occurrence indices (6 cell + pair, 4 cell + column) fit 31 bits (at most
+// kMaxCells cells): pass A computes them in 32-bit arithmetic (in pass B the
+// 64-bit forms keep its register allocation free of spills).
+__device__ __forceinline__ void set_bit(uint32_t *bits, int p)
 {
     atomicOr(bits + (p >> 5), 1u << (p & 31));
 }
@@ -356,7 +359,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
                 const int ko = cand_of(o, sv);      // the omitted candidate
                 const M mf = ko == 0 ? cm[1] & cm[2] : (ko == 1 ? cm[0] & cm[2] : cm[0] & cm[1]);
                 if (mctz(mf) != pos) continue;
-                const long long q = 4LL * c + (3 - o);
+                const int q = 4 * c + (3 - o);
                 set_bit(a.fflag, q);
                 const int ncell = mpopc(mf);
                 if (ncell == 1) set_bit(a.fbnd, q);
@@ -379,7 +382,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
         const int i = tt / L, sub = tt % L;
         int n_ef = 0;
         M mu = 0;
-        long long p = 0;
+        int p = 0;
         if (i < nw) {
             const int e = work[i] >> 2, k = work[i] & 3;
             const int m = S.meta[e];
@@ -387,7 +390,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
             const int t = k + (k >= sv);
             const int u = get4(S.tv[e], t);
             mu = S.hmask[S.cslot[e][k]];
-            p = 6LL * S.cell[e] + pair_slot(sv, t);
+            p = 6 * S.cell[e] + pair_slot(sv, t);
             M mm = mu;
             for (int q = 0; q < sub; q++) mm &= mm - 1;
             while (mm) {
