@@ -13,7 +13,8 @@ vertices), vertex ids permuted, float32 field = 32 Gaussians + N(0, 1e-3).
          (a 512 MB write) before every step, outside the timed window.
   e2e    the same steps through the C ABI with HOST buffers: pinned TV and
          field copied in, and every relation plus the classes copied back to
-         pinned host memory (tg_copy_relation_async), all inside the timed
+         pinned host memory (tg_copy_relations_async_i32: CSR offsets as
+         int32, narrowed on the device by one launch), all inside the timed
          window.  Steps alternate between two streams and two sets of host
          buffers, so a step's copies back overlap the next step's extraction
          (the host link, not the kernels, bounds this number).
@@ -371,6 +372,7 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
                 if k + 1 < n_steps:
                     upload(k + 1)
                 u = lib.tg_batch_union(b._h)
+                po, pe = (C.c_void_p * 14)(), (C.c_void_p * 14)()
                 for n in tg.RELATIONS[1:]:
                     off, ent = C.c_void_p(), C.c_void_p()
                     rows, cnt, width = C.c_int64(), C.c_int64(), C.c_int32()
@@ -380,12 +382,12 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
                     hb = h_bufs[k % 2]
                     if n not in hb:
                         hb[n] = (torch.empty(max(cnt.value, 1), dtype=torch.int32).pin_memory(),
-                                 torch.empty(rows.value + 1, dtype=torch.int64).pin_memory()
+                                 torch.empty(rows.value + 1, dtype=torch.int32).pin_memory()
                                  if width.value == 0 else None)
                     he, ho = hb[n]
-                    tg._lib.check(lib.tg_copy_relation_async(
-                        u, tg.REL[n], ho.data_ptr() if ho is not None else None,
-                        he.data_ptr() if cnt.value else None, es))
+                    pe[tg.REL[n]] = he.data_ptr() if cnt.value else None
+                    po[tg.REL[n]] = ho.data_ptr() if ho is not None else None
+                tg._lib.check(lib.tg_copy_relations_async_i32(u, tg.ALL_RELATIONS, po, pe, es))
                 with torch.cuda.stream(e_streams[k % 2]):
                     h_cls[k % 2].copy_(d_cls2[k % 2], non_blocking=True)
                 if live is not None:
@@ -396,7 +398,7 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
             torch.cuda.synchronize()
 
         e2e_run(2)
-        d2h += sum(a.numel() * 4 + (bb.numel() * 8 if bb is not None else 0)
+        d2h += sum(a.numel() * 4 + (bb.numel() * 4 if bb is not None else 0)
                    for a, bb in h_bufs[0].values())
         t0 = time.perf_counter()
         e2e_run(args.e2e_steps)
@@ -668,12 +670,21 @@ def main():
                  for n, (r, w) in fixed_rows.items()}
         h_ent.update({n: torch.empty(max(totals[n], 1), dtype=torch.int32).pin_memory()
                       for n in csr_rows})
-        h_off = {n: torch.empty(r + 1, dtype=torch.int64).pin_memory() for n, r in csr_rows.items()}
+        h_off = {n: torch.empty(r + 1, dtype=torch.int32).pin_memory() for n, r in csr_rows.items()}
         h_cls = torch.empty(3 * V, dtype=torch.int32).pin_memory()
         bufs.append((h_ent, h_off, h_cls))
+    ptr_off, ptr_ent = [], []
+    for h_ent, h_off, _ in bufs:
+        po, pe = (tg._lib.C.c_void_p * 14)(), (tg._lib.C.c_void_p * 14)()
+        for n in names:
+            pe[tg.REL[n]] = h_ent[n].data_ptr()
+            if n in h_off:
+                po[tg.REL[n]] = h_off[n].data_ptr()
+        ptr_off.append(po)
+        ptr_ent.append(pe)
     h2d = pin_tv.numel() * 4 + pin_field.numel() * 4
     d2h = sum(r * w * 4 for r, w in fixed_rows.values()) + sum(totals[n] * 4 for n in csr_rows) \
-        + sum((r + 1) * 8 for r in csr_rows.values()) + V * 12
+        + sum((r + 1) * 4 for r in csr_rows.values()) + V * 12
     lib = tg.load()
     dev = f"cuda:{local_rank}"
     e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
@@ -700,10 +711,10 @@ def main():
                                                  d_cls2[k % 2].data_ptr(), 1, es))
             if k + 1 < n_steps:
                 upload(k + 1)
-            for n in names:
-                tg._lib.check(lib.tg_copy_relation_async(
-                    g._h, tg.REL[n], h_off[n].data_ptr() if n in h_off else None,
-                    h_ent[n].data_ptr(), es))
+            # every relation through one call: CSR offsets narrowed to int32
+            # by one launch, then the copies back to back
+            tg._lib.check(lib.tg_copy_relations_async_i32(g._h, tg.ALL_RELATIONS,
+                                                          ptr_off[k % 2], ptr_ent[k % 2], es))
             with torch.cuda.stream(e_streams[k % 2]):
                 h_cls.copy_(d_cls2[k % 2], non_blocking=True)
             if live is not None:

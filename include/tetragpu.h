@@ -140,6 +140,26 @@ tg_status tg_copy_relation(const tg_mesh *mesh, int relation, int64_t *offsets_h
  * stream, or synchronise the stream before reading the buffers). */
 tg_status tg_copy_relation_async(tg_mesh *mesh, int relation, int64_t *offsets_host,
                                  int32_t *entries_host, void *stream);
+/* tg_copy_relation_async with a CSR relation's offsets narrowed to int32 on
+ * the device first: half the offset bytes over the host link (the
+ * reference's device_VV row index is 32-bit as well,
+ * src/cuda_extraction.cu:1180-1274).  A relation of 2^31 or more entries is
+ * refused with TG_ERR_UNSUPPORTED; fixed-width relations copy their entries
+ * only. */
+tg_status tg_copy_relation_async_i32(tg_mesh *mesh, int relation, int32_t *offsets_host,
+                                     int32_t *entries_host, void *stream);
+/* The same, synchronous with respect to the host. */
+tg_status tg_copy_relation_i32(tg_mesh *mesh, int relation, int32_t *offsets_host,
+                               int32_t *entries_host, void *stream);
+/* Every relation in relation_mask (TG_TE | TG_EV | ...) at once, as
+ * tg_copy_relation_async_i32 does one: offsets_host[r] and entries_host[r]
+ * (arrays of 14 pointers indexed by relation, NULL to skip one) receive
+ * relation r.  The offsets of all requested CSR relations are narrowed by one
+ * launch before any copy is issued, so the copies follow one another on the
+ * copy engine without waiting for kernels between them. */
+tg_status tg_copy_relations_async_i32(tg_mesh *mesh, uint32_t relation_mask,
+                                      int32_t *const *offsets_host,
+                                      int32_t *const *entries_host, void *stream);
 
 /* A relation's entries widened to int64 (the reference's vtkIdType) and its
  * int64 offsets (CSR only; may be NULL), into caller memory on the device

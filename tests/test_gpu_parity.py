@@ -184,3 +184,52 @@ def test_large_mesh_properties(gpu_lib):
         assert set(np.unique(cp[:, 2])) <= {1, 2, 3, 4}
         regular = cp[:, 2] == 3
         assert ((cp[regular, 0] == 1) & (cp[regular, 1] == 1)).all()
+
+
+def test_int32_offset_copies_match(gpu_lib):
+    """tg_copy_relation_i32: every CSR relation's offsets narrowed to int32
+    equal the int64 ones, entries identical; fixed-width relations refused by
+    the Python helper."""
+    m = meshgen.kuhn_mesh((5, 4, 6), 0.3, seed=77)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        g.extract(gpu_lib.ALL_RELATIONS)
+        for name in ("ET", "EF", "VT", "TT", "FF", "EE", "VV"):
+            off64, ent64 = g.relation(name)
+            off32, ent32 = g.relation_i32(name)
+            assert off32.dtype == np.int32 and np.array_equal(off32.astype(np.int64), off64), name
+            assert np.array_equal(ent32, ent64), name
+        with pytest.raises(ValueError):
+            g.relation_i32("TE")
+
+
+def test_relations_copied_at_once_with_int32_offsets(gpu_lib):
+    """tg_copy_relations_async_i32: all 13 relations in one call (one
+    narrowing launch, then the copies) equal the per-relation int64 copies."""
+    import ctypes as C
+    import torch
+    from tetragpu_gb300._lib import check
+    m = meshgen.kuhn_mesh((4, 6, 5), 0.25, seed=78)
+    with gpu_lib.Mesh(m.tv, m.n_verts) as g:
+        g.extract(gpu_lib.ALL_RELATIONS)
+        offs, ents = (C.c_void_p * 14)(), (C.c_void_p * 14)()
+        got, mask = {}, 0
+        for name in RELS:
+            d = g.device_relation(name)
+            r = gpu_lib.REL[name]
+            mask |= 1 << r
+            ent = np.empty(max(d["n_entries"], 1), dtype=np.int32)
+            ents[r] = ent.ctypes.data
+            off = None
+            if d["width"] == 0:
+                off = np.empty(d["rows"] + 1, dtype=np.int32)
+                offs[r] = off.ctypes.data
+            got[name] = (off, ent, d)
+        check(g._lib.tg_copy_relations_async_i32(g._h, mask, offs, ents, None))
+        torch.cuda.synchronize()
+        for name, (off, ent, d) in got.items():
+            want = g.relation(name)
+            if d["width"] > 0:
+                assert np.array_equal(ent[:d["n_entries"]].reshape(d["rows"], d["width"]), want), name
+            else:
+                assert np.array_equal(off.astype(np.int64), want[0]), name
+                assert np.array_equal(ent[:d["n_entries"]], want[1]), name

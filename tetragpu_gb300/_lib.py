@@ -63,6 +63,9 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_get_relation": (C.c_int, [vp, C.c_int, P(vp), P(vp), P(i64), P(i64), P(i32)]),
         "tg_copy_relation": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "tg_copy_relation_async": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "tg_copy_relation_async_i32": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "tg_copy_relation_i32": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "tg_copy_relations_async_i32": (C.c_int, [vp, u32, vp, vp, vp]),
         "tg_get_tv": (C.c_int, [vp, P(vp)]),
         "tg_export_relation_i64": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp]),
         "tg_export_rows_padded": (C.c_int, [vp, C.c_int, i32, vp, vp, vp]),
@@ -183,6 +186,18 @@ class Mesh:
         off = np.empty(d["rows"] + 1, dtype=np.int64)
         check(self._lib.tg_copy_relation(self._h, REL[name], off.ctypes.data,
                                          ent.ctypes.data if ent.size else None, _stream(stream)))
+        return off, ent
+
+    def relation_i32(self, name: str):
+        """Host copy of a CSR relation with int32 offsets (narrowed on the
+        device): (offsets int32, entries int32)."""
+        d = self.device_relation(name)
+        if d["width"] > 0:
+            raise ValueError(f"{name} is fixed-width: use relation()")
+        off = np.empty(d["rows"] + 1, dtype=np.int32)
+        ent = np.empty(d["n_entries"], dtype=np.int32)
+        check(self._lib.tg_copy_relation_i32(self._h, REL[name], off.ctypes.data,
+                                             ent.ctypes.data if ent.size else None, None))
         return off, ent
 
     def tv_sorted_ptr(self) -> int:

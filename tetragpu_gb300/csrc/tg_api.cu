@@ -788,6 +788,84 @@ tg_status tg_copy_relation_async(tg_mesh *m, int r, int64_t *off_host, int32_t *
     return TG_OK;
 }
 
+tg_status tg_copy_relation_async_i32(tg_mesh *m, int r, int32_t *off_host, int32_t *ent_host,
+                                     void *stream)
+{
+    if (!m || r < 1 || r > 13) return fail(TG_ERR_INVALID_ARGUMENT, "bad mesh or relation index");
+    const Rel &x = m->rel[r];
+    if (!x.ready) return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+    cudaStream_t s = (cudaStream_t)stream;
+    m->last_stream = s;
+    if (off_host && x.off) {
+        if (x.entries > INT32_MAX)
+            return fail(TG_ERR_UNSUPPORTED, "relation %s has %lld entries: its offsets need int64",
+                        kName[r], (long long)x.entries);
+        int32_t *d = nullptr;
+        const size_t b = (size_t)(x.rows + 1) * 4;
+        CK(cudaMallocAsync(&d, b, s));
+        launch_narrow(x.off, d, x.rows + 1, s);
+        const cudaError_t e = cudaMemcpyAsync(off_host, d, b, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(d, s);   // stream-ordered: after the copy
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (offsets)", __LINE__);
+    }
+    if (ent_host && x.entries)
+        CK(cudaMemcpyAsync(ent_host, x.ent, (size_t)x.entries * 4, cudaMemcpyDeviceToHost, s));
+    return TG_OK;
+}
+
+tg_status tg_copy_relations_async_i32(tg_mesh *m, uint32_t mask, int32_t *const *off_host,
+                                      int32_t *const *ent_host, void *stream)
+{
+    if (!m || !off_host || !ent_host) return fail(TG_ERR_INVALID_ARGUMENT, "NULL argument");
+    mask &= TG_ALL_RELATIONS;
+    cudaStream_t s = (cudaStream_t)stream;
+    m->last_stream = s;
+    NarrowJobs j{};
+    int64_t at[14] = {};
+    for (int r = 1; r < 14; r++) {
+        if (!(mask & bit(r))) continue;
+        const Rel &x = m->rel[r];
+        if (!x.ready)
+            return fail(TG_ERR_NOT_COMPUTED, "relation %s has not been extracted", kName[r]);
+        if (!off_host[r] || !x.off) continue;
+        if (x.entries > INT32_MAX)
+            return fail(TG_ERR_UNSUPPORTED, "relation %s has %lld entries: its offsets need int64",
+                        kName[r], (long long)x.entries);
+        at[r] = j.start[j.n];
+        j.src[j.n] = x.off;
+        j.start[j.n + 1] = j.start[j.n] + x.rows + 1;
+        j.n++;
+    }
+    int32_t *d = nullptr;
+    if (j.n > 0) {
+        CK(cudaMallocAsync(&d, (size_t)j.start[j.n] * 4, s));
+        j.dst = d;
+        launch_narrow_multi(j, s);
+    }
+    cudaError_t e = cudaSuccess;
+    for (int r = 1; r < 14 && e == cudaSuccess; r++) {
+        if (!(mask & bit(r))) continue;
+        const Rel &x = m->rel[r];
+        if (off_host[r] && x.off)
+            e = cudaMemcpyAsync(off_host[r], d + at[r], (size_t)(x.rows + 1) * 4,
+                                cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && ent_host[r] && x.entries)
+            e = cudaMemcpyAsync(ent_host[r], x.ent, (size_t)x.entries * 4, cudaMemcpyDeviceToHost,
+                                s);
+    }
+    if (d) cudaFreeAsync(d, s);   // stream-ordered: after the copies
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (relations)", __LINE__);
+    return TG_OK;
+}
+
+tg_status tg_copy_relation_i32(tg_mesh *m, int r, int32_t *off_host, int32_t *ent_host,
+                               void *stream)
+{
+    TRY(tg_copy_relation_async_i32(m, r, off_host, ent_host, stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    return TG_OK;
+}
+
 tg_status tg_export_relation_i64(const tg_mesh *m, int r, int64_t *entries_out,
                                  int64_t *offsets_out, int out_on_device, void *stream)
 {

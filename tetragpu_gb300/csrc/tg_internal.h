@@ -73,6 +73,15 @@ struct PublishArgs {
 };
 void launch_publish(const PublishArgs &a, cudaStream_t s);
 void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s);
+void launch_narrow(const int64_t *src, int32_t *dst, int64_t n, cudaStream_t s);
+// up to 16 int64 arrays narrowed into one int32 array, back to back
+struct NarrowJobs {
+    const int64_t *src[16];
+    int64_t start[17];   // start[k]: first output element of array k; start[n] = total
+    int n;
+    int32_t *dst;
+};
+void launch_narrow_multi(const NarrowJobs &j, cudaStream_t s);
 void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
                      int64_t *out, uint32_t *counts, cudaStream_t s);
 // sort each TV row, validate ids, count cells per vertex; occ[c] = the

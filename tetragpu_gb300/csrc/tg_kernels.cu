@@ -480,6 +480,26 @@ k_widen(const int *__restrict__ src, long long *__restrict__ dst, int64_t n)
         dst[i] = src[i];
 }
 
+// int64 -> int32 copy (CSR offsets of a relation below 2^31 entries)
+__global__ void __launch_bounds__(256)
+k_narrow(const int64_t *__restrict__ src, int *__restrict__ dst, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (int)src[i];
+}
+
+__global__ void __launch_bounds__(256) k_narrow_multi(NarrowJobs j)
+{
+    const int64_t total = j.start[j.n];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int k = 0;
+        while (i >= j.start[k + 1]) k++;
+        j.dst[i] = (int)j.src[k][i - j.start[k]];
+    }
+}
+
 // CSR rows -> the reference's padded device_VV layout: row v at v * width,
 // unused slots -1, plus the row lengths
 __global__ void __launch_bounds__(256)
@@ -521,6 +541,23 @@ void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s)
     Launch L("k_widen", s);
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
     k_widen<<<(unsigned)blocks, 256, 0, s>>>(src, reinterpret_cast<long long *>(dst), n);
+}
+
+void launch_narrow(const int64_t *src, int32_t *dst, int64_t n, cudaStream_t s)
+{
+    if (n == 0) return;
+    Launch L("k_narrow", s);
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
+    k_narrow<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n);
+}
+
+void launch_narrow_multi(const NarrowJobs &j, cudaStream_t s)
+{
+    const int64_t n = j.start[j.n];
+    if (n == 0) return;
+    Launch L("k_narrow_multi", s);
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
+    k_narrow_multi<<<(unsigned)blocks, 256, 0, s>>>(j);
 }
 
 void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
