@@ -218,6 +218,19 @@ tg_status dalloc(T **out, int64_t count, cudaStream_t s)
     return TG_OK;
 }
 
+// Offsets of several arrays in one allocation (each on a 256-byte boundary),
+// so that arrays zeroed together cost one memset.
+struct Carve {
+    size_t bytes = 0;
+    template <class T>
+    size_t add(int64_t n)
+    {
+        const size_t off = bytes;
+        bytes += ((size_t)std::max<int64_t>(n, 1) * sizeof(T) + 255) & ~size_t(255);
+        return off;
+    }
+};
+
 }  // namespace
 
 void tg::set_last_error(const char *msg) { g_err = msg; }
@@ -234,6 +247,7 @@ struct tg_mesh {
     int32_t *vtp = nullptr;             // [4T] VT rows in that order
     int32_t *st_win = nullptr;          // window table over pofs (star pass A)
     int32_t *st_win_b = nullptr;        // the same for star pass B's windows
+    ScanWorkspace scan;                 // every prefix scan of the mesh (tg_scan.cu)
     // segments of cells (the meshes of a batch): cell starts, and after each
     // extraction their first edge and face ids (device, n_seg + 1 each)
     int64_t n_seg = 0;
@@ -310,6 +324,8 @@ tg_status check_flags(const tg_mesh *m, unsigned mask_ok = 0)
         return fail(TG_ERR_UNSUPPORTED, "vertex %d: neighbour table overflow", h.bad_vertex);
     if (f & ST_STAR_OVERFLOW)
         return fail(TG_ERR_UNSUPPORTED, "vertex %d: neighbour summary overflow", h.bad_vertex);
+    if (f & ST_SCAN_STALLED)
+        return fail(TG_ERR_CUDA, "a prefix scan gave up waiting for a preceding tile");
     return fail(TG_ERR_CUDA, "unexpected device status 0x%x", f);
 }
 
@@ -363,19 +379,26 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         int32_t *deg;
         int64_t *vv_off;
         const bool need_ecnt = mask & (TG_ET | TG_EF | TG_EE);
-        TRY(tmp.alloc(&eflag, nwe, true));
-        TRY(tmp.alloc(&fflag, nwf, true));
-        TRY(tmp.alloc(&fbnd, nwf, true));
+        {
+            // the bitmaps pass A sets bits in and the neighbour counts: one
+            // zeroed allocation (the row lengths are read only where pass A
+            // wrote them: no zeroing)
+            Carve c;
+            const size_t o_e = c.add<uint32_t>(nwe), o_f = c.add<uint32_t>(nwf),
+                         o_b = c.add<uint32_t>(nwf), o_d = c.add<int32_t>(V);
+            char *z;
+            TRY(tmp.alloc(&z, (int64_t)c.bytes, true));
+            eflag = (uint32_t *)(z + o_e);
+            fflag = (uint32_t *)(z + o_f);
+            fbnd = (uint32_t *)(z + o_b);
+            deg = (int32_t *)(z + o_d);
+        }
         TRY(tmp.alloc(&erank, nwe + 1));
         TRY(tmp.alloc(&frank, nwf + 1));
         TRY(tmp.alloc(&brank, nwf + 1));
-        if (need_ecnt) TRY(tmp.alloc(&ecnt, 6 * T, true));
-        TRY(tmp.alloc(&deg, V, true));
+        if (need_ecnt) TRY(tmp.alloc(&ecnt, 6 * T));
         TRY(dalloc(&vv_off, V + 1, s));
         tmp.track(vv_off);  // owned by the VV relation once it is ready
-        char *scratch;
-        const int64_t maxn = std::max(V, std::max(nwe, nwf));
-        TRY(tmp.alloc(&scratch, 5 * (int64_t)(scan_scratch_bytes(maxn) + 256)));
         int64_t *deg_sq;  // prefix of deg^2: its total sizes EE (sum deg^2 - 2E)
         TRY(tmp.alloc(&deg_sq, V + 1));
         uint64_t *emask;  // pass A's candidate masks, pass B's input
@@ -393,7 +416,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
                            {fflag, frank, nwf, SCAN_POPC_RANK, 0},
                            {fbnd, brank, nwf, SCAN_POPC_RANK, 0},
                            {deg, deg_sq, V, SCAN_SQUARE_I32, 0}};
-        scan_batch(jobs, 5, scratch, s);
+        scan_batch(jobs, 5, m->scan, m->st, s);
 
         // ---- the one synchronisation: edge, face, neighbour and boundary
         // counts size every output from here on ----
@@ -524,10 +547,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         TRY(tmp.alloc(&cnt, T));
         TRY(dalloc(&tt_off, T + 1, s));
         launch_tt_vertex_count(m->tvs, T, vt_off, vt, cnt, s);
-        char *scratch;
-        TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(T) + 256));
         ScanJob job{cnt, tt_off, T, SCAN_COUNT_I32, 0};
-        scan_batch(&job, 1, scratch, s);
+        scan_batch(&job, 1, m->scan, m->st, s);
         const void *src[1] = {tt_off + T};
         const bool w8[1] = {true};
         TRY(sync_read(m, s, 1, src, w8));
@@ -613,7 +634,13 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     if (m->seg_ef) cudaFreeAsync(m->seg_ef, s);
     if (m->cadj) cudaFreeAsync(m->cadj, s);
     if (m->st) cudaFreeAsync(m->st, s);
+    if (m->scan.buf) {
+        // after the last scan, whichever stream it ran on
+        if (m->scan.used && m->scan.last != s) cudaStreamWaitEvent(s, m->scan.done, 0);
+        cudaFreeAsync(m->scan.buf, s);
+    }
     cudaStreamSynchronize(s);  // no copy into the pinned slots is still in flight
+    if (m->scan.done) cudaEventDestroy(m->scan.done);
     g_pinned.put(m->st_host);
     g_pinned.put(m->sz_host);
     cudaSetDevice(cur);
@@ -638,44 +665,55 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
         CK(cudaMemcpyAsync(m->tvs, tv, (size_t)T * 16, cudaMemcpyHostToDevice, s));
         src = reinterpret_cast<const int32_t *>(m->tvs);
     }
+    // the scan workspace of every later scan on the mesh, zeroed once
+    m->scan.job_words = scan_job_words(std::max(std::max(V, T), (6 * T + 31) / 32));
+    const size_t ws_bytes = (size_t)2 * kMaxScanJobs * m->scan.job_words * 8;
+    CK(cudaMallocAsync((void **)&m->scan.buf, ws_bytes, s));
+    CK(cudaMemsetAsync(m->scan.buf, 0, ws_bytes, s));
+    CK(cudaEventCreateWithFlags(&m->scan.done, cudaEventDisableTiming));
     Temps tmp(s);
+    // the per-vertex cell counts and the first-cell bitmap: one zeroed
+    // allocation
+    const int64_t nwk = (4 * T + 31) / 32;
     int32_t *deg_t;
+    uint32_t *vflag;
+    {
+        Carve c;
+        const size_t o_d = c.add<int32_t>(V), o_f = c.add<uint32_t>(nwk);
+        char *z;
+        TRY(tmp.alloc(&z, (int64_t)c.bytes, true));
+        deg_t = (int32_t *)(z + o_d);
+        vflag = (uint32_t *)(z + o_f);
+    }
     int4 *occ;
-    TRY(tmp.alloc(&deg_t, V, true));
     TRY(tmp.alloc(&occ, T));
     launch_canon(src, T, V, m->tvs, deg_t, occ, m->st, s);
     int64_t *vt_off;
     int32_t *vt;
     TRY(dalloc(&vt_off, V + 1, s));
-    char *scratch;
-    TRY(tmp.alloc(&scratch, (int64_t)scan_scratch_bytes(std::max(V, (4 * T + 31) / 32)) + 256));
     ScanJob job{deg_t, vt_off, V, SCAN_COUNT_I32, 0};
-    scan_batch(&job, 1, scratch, s);
+    scan_batch(&job, 1, m->scan, m->st, s);
     TRY(dalloc(&vt, 4 * T, s));
     launch_vt_fill(m->tvs, T, vt_off, occ, vt, s);
     TRY(dalloc(&m->vt_win, window_count(4 * T, star_window()) + 1, s));
     launch_window_starts(vt_off, V, 4 * T, star_window(), m->vt_win, s);
     // VT row sort, which also marks each vertex's star-order key; then the
     // star processing order: positions, row lengths, offsets, rows, windows
-    const int64_t nwk = (4 * T + 31) / 32;
-    uint32_t *vflag;
     uint2 *vrank;
     int64_t *vkey;
     int32_t *dcount;
-    TRY(tmp.alloc(&vflag, nwk, true));
     TRY(tmp.alloc(&vrank, nwk + 1));
     TRY(tmp.alloc(&vkey, V));
-    TRY(tmp.alloc(&dcount, V, true));
+    TRY(tmp.alloc(&dcount, V));
     launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, m->tvs, vflag, vkey, s);
     {
         ScanJob jf{vflag, vrank, nwk, SCAN_POPC_RANK, 0};
-        scan_batch(&jf, 1, scratch, s);
+        scan_batch(&jf, 1, m->scan, m->st, s);
         TRY(dalloc(&m->vorder, V, s));
-        CK(cudaMemsetAsync(m->vorder, 0, (size_t)std::max<int64_t>(V, 1) * 4, s));
-        launch_vorder_place(vt_off, V, vkey, vrank, m->vorder, dcount, s);
+        launch_vorder_place(vt_off, V, vkey, vrank, nwk, m->vorder, dcount, s);
         TRY(dalloc(&m->pofs, V + 1, s));
         ScanJob jd{dcount, m->pofs, V, SCAN_COUNT_I32, 0};
-        scan_batch(&jd, 1, scratch, s);
+        scan_batch(&jd, 1, m->scan, m->st, s);
         TRY(dalloc(&m->vtp, 4 * T, s));
         launch_vtp_fill(m->vorder, m->pofs, V, vt_off, vt, m->vtp, s);
         TRY(dalloc(&m->st_win, window_count(4 * T, star_window()) + 1, s));

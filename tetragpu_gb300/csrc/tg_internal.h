@@ -27,7 +27,8 @@ enum StatusFlag : unsigned int {
     ST_STAR_OVERFLOW = 8u,     // more neighbours than the summary slot holds
     ST_NONMANIFOLD_FACE = 16u, // a face lies in more than two cells
     ST_HASH_FULL = 32u,        // per-vertex neighbour table overflowed
-    ST_HEAVY_DEG = 64u         // a vertex has more neighbours than the kernels hold
+    ST_HEAVY_DEG = 64u,        // a vertex has more neighbours than the kernels hold
+    ST_SCAN_STALLED = 128u     // a scan tile gave up waiting for the tiles before it
 };
 
 // Largest star (cells around one vertex) and neighbourhood handled on the
@@ -50,10 +51,22 @@ struct ScanJob {
     int pad;
 };
 constexpr int kMaxScanJobs = 8;
-// Exclusive scans of up to kMaxScanJobs arrays in three launches.  `scratch`
-// must hold scan_scratch_bytes(max n) bytes per job.
-size_t scan_scratch_bytes(int64_t n);
-void scan_batch(const ScanJob *jobs, int n_jobs, void *scratch, cudaStream_t s);
+// Exclusive scans of up to kMaxScanJobs arrays in one launch, over a
+// workspace of two buffers of kMaxScanJobs * job_words words (zeroed once when
+// made): a scan uses one buffer and zeroes the other for the next scan, so no
+// scan needs a memset.  A scan issued on another stream than the last one
+// waits for the last one first (event `done`).  A stalled scan sets
+// ST_SCAN_STALLED in st.
+struct ScanWorkspace {
+    unsigned long long *buf = nullptr;   // 2 * kMaxScanJobs * job_words words
+    int64_t job_words = 0;               // tile words + ticket of the longest array
+    int cur = 0;
+    cudaEvent_t done = nullptr;
+    cudaStream_t last = nullptr;
+    bool used = false;
+};
+int64_t scan_job_words(int64_t max_n);
+void scan_batch(const ScanJob *jobs, int n_jobs, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
 
 // ---- pipeline kernels (tg_kernels.cu) ----
 struct Sizes {
@@ -109,7 +122,8 @@ void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int6
 // dcount[pos] = its row length, pos = rank of its key; vtp = VT rows in that
 // order, pofs = its offsets (rows with no cells last, length 0)
 void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
-                         const uint2 *vrank, int32_t *vorder, int32_t *dcount, cudaStream_t s);
+                         const uint2 *vrank, int64_t nwk, int32_t *vorder, int32_t *dcount,
+                         cudaStream_t s);
 void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
                      const int32_t *vt, int32_t *vtp, cudaStream_t s);
 

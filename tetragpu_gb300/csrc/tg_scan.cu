@@ -1,10 +1,15 @@
-// tg_scan.cu -- batched exclusive scans (reduce, scan partials, downsweep).
+// tg_scan.cu -- batched exclusive scans in one pass (decoupled look-back).
 //
 // Every CSR offset array and every bit-rank prefix of the pipeline comes out
-// of here.  Up to kMaxScanJobs independent arrays are scanned by the same
-// three launches (blockIdx.y selects the array), so a stage that produces
-// five count arrays pays three launches, not fifteen.  No spin-waits: the
-// partial sums go through global memory between launches.
+// of here.  Up to kMaxScanJobs independent arrays are scanned by one launch
+// (blockIdx.y selects the array), reading each input once.  A block takes the
+// next tile of its array in start order (a ticket), sums the tile, publishes
+// the sum, and adds the published sums of the tiles before it until it meets
+// one whose inclusive prefix is already known (Merrill and Garland's
+// single-pass scan).  A block waits only on tiles whose blocks started before
+// it, so every wait ends; it is bounded all the same: after kLookbackPolls
+// polls the block records ST_SCAN_STALLED in the mesh status (reported at the
+// next status read-back) and goes on.
 #include "tg_internal.h"
 
 namespace tg {
@@ -14,9 +19,17 @@ constexpr int kThreads = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;  // 2048 elements per tile
 
+constexpr unsigned kLookbackPolls = 1u << 16;
+
 struct ScanParams {
     ScanJob job[kMaxScanJobs];
-    int64_t *partials[kMaxScanJobs];
+    // per array: one word per tile (sum << 2 | 1 once the tile's sum is
+    // published, inclusive prefix << 2 | 2 once that is known, 0 before),
+    // then the ticket counter; zeroed before the launch
+    unsigned long long *tiles[kMaxScanJobs];
+    unsigned long long *next;   // the other buffer, zeroed here for the next scan
+    int64_t next_words;
+    unsigned *err;
     int n_jobs;
 };
 
@@ -68,67 +81,59 @@ __device__ __forceinline__ int64_t block_exclusive_scan(int64_t x, int64_t &excl
     return total;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_reduce(ScanParams p)
+// Publish tile `tile`'s sum and return the sum of the tiles before it.
+__device__ __forceinline__ int64_t look_back(unsigned long long *w, int64_t tile, int64_t sum,
+                                             unsigned *err)
 {
-    const int jb = blockIdx.y;
-    if (jb >= p.n_jobs) return;
-    const ScanJob &j = p.job[jb];
-    const int64_t ntiles = (j.n + kTile - 1) / kTile;
-    const int64_t tile = blockIdx.x;
-    if (tile >= ntiles) return;
-    const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
-    int64_t s = 0;
-#pragma unroll
-    for (int k = 0; k < kItems; k++)
-        if (base + k < j.n) s += load_value(j, base + k);
-    __shared__ int64_t sm[kThreads / 32 + 1];
-    int64_t excl;
-    int64_t total = block_exclusive_scan<kThreads>(s, excl, sm);
-    if (threadIdx.x == 0) p.partials[jb][tile] = total;
-}
-
-__global__ void __launch_bounds__(1024) k_scan_partials(ScanParams p)
-{
-    const int jb = blockIdx.x;
-    if (jb >= p.n_jobs) return;
-    const ScanJob &j = p.job[jb];
-    const int64_t ntiles = (j.n + kTile - 1) / kTile;
-    int64_t *part = p.partials[jb];
-    __shared__ int64_t sm[1024 / 32 + 1];
-    // chunks of 8192 tiles: a thread loads eight consecutive partials at
-    // once, one block-wide scan of the thread sums per chunk
-    constexpr int kPer = 8;
-    int64_t carry = 0;
-    for (int64_t b = 0; b < ntiles; b += 1024 * kPer) {
-        const int64_t i0 = b + (int64_t)threadIdx.x * kPer;
-        int64_t v[kPer], x = 0;
-#pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            v[k] = i0 + k < ntiles ? part[i0 + k] : 0;
-            x += v[k];
-        }
-        int64_t run;
-        const int64_t tot = block_exclusive_scan<1024>(x, run, sm);
-        run += carry;
-#pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            if (i0 + k < ntiles) part[i0 + k] = run;
-            run += v[k];
-        }
-        carry += tot;
+    if (tile == 0) {
+        atomicExch(w, ((unsigned long long)sum << 2) | 2ull);
+        return 0;
     }
-    const int64_t total = carry;
-    if (threadIdx.x == 0) store_value(j, j.n, total);
+    atomicExch(w + tile, ((unsigned long long)sum << 2) | 1ull);
+    int64_t prefix = 0;
+    int64_t k = tile - 1;
+    unsigned polls = 0;
+    while (true) {
+        const unsigned long long x = *reinterpret_cast<volatile unsigned long long *>(w + k);
+        const unsigned f = (unsigned)(x & 3ull);
+        if (f == 0) {   // tile k's block has not published yet
+            if (++polls > kLookbackPolls) {
+                atomicOr(err, ST_SCAN_STALLED);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        prefix += (int64_t)(x >> 2);
+        if (f == 2) break;   // an inclusive prefix: done (tile 0 always has one)
+        --k;
+    }
+    atomicExch(w + tile, ((unsigned long long)(prefix + sum) << 2) | 2ull);
+    return prefix;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_down(ScanParams p)
+__global__ void __launch_bounds__(kThreads) k_scan(ScanParams p)
 {
     const int jb = blockIdx.y;
     if (jb >= p.n_jobs) return;
     const ScanJob &j = p.job[jb];
     const int64_t ntiles = (j.n + kTile - 1) / kTile;
-    const int64_t tile = blockIdx.x;
-    if (tile >= ntiles) return;
+    unsigned long long *w = p.tiles[jb];
+    {
+        const int64_t nthreads = (int64_t)gridDim.x * gridDim.y * blockDim.x;
+        const int64_t t0 = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        for (int64_t i = t0; i < p.next_words; i += nthreads) p.next[i] = 0ull;
+    }
+    __shared__ int64_t sm[kThreads / 32 + 1];
+    __shared__ int64_t s_tile, s_prefix;
+    if (threadIdx.x == 0) s_tile = (int64_t)atomicAdd(w + ntiles, 1ull);   // the ticket
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (ntiles == 0) {   // an empty array: its total alone
+        if (tile == 0 && threadIdx.x == 0) store_value(j, 0, 0);
+        return;
+    }
+    if (tile >= ntiles) return;   // a surplus block of a shorter array
     const int64_t base = tile * kTile + (int64_t)threadIdx.x * kItems;
     int64_t v[kItems];
     int64_t s = 0;
@@ -137,57 +142,52 @@ __global__ void __launch_bounds__(kThreads) k_scan_down(ScanParams p)
         v[k] = (base + k < j.n) ? load_value(j, base + k) : 0;
         s += v[k];
     }
-    __shared__ int64_t sm[kThreads / 32 + 1];
     int64_t excl;
-    block_exclusive_scan<kThreads>(s, excl, sm);
-    int64_t run = p.partials[jb][tile] + excl;
+    const int64_t total = block_exclusive_scan<kThreads>(s, excl, sm);
+    if (threadIdx.x == 0) s_prefix = look_back(w, tile, total, p.err);
+    __syncthreads();
+    int64_t run = s_prefix + excl;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         if (base + k < j.n) store_value(j, base + k, run);
         run += v[k];
     }
+    if (tile == ntiles - 1 && threadIdx.x == 0) store_value(j, j.n, s_prefix + total);
 }
 
 }  // namespace
 
-size_t scan_scratch_bytes(int64_t n)
+int64_t scan_job_words(int64_t max_n)
 {
-    int64_t ntiles = (n + kTile - 1) / kTile;
-    return (size_t)(ntiles + 1) * sizeof(int64_t);
+    return (max_n + kTile - 1) / kTile + 1;
 }
 
-void scan_batch(const ScanJob *jobs, int n_jobs, void *scratch, cudaStream_t s)
+void scan_batch(const ScanJob *jobs, int n_jobs, ScanWorkspace &ws, DevStatus *st, cudaStream_t s)
 {
     if (n_jobs <= 0) return;
     ScanParams p{};
     p.n_jobs = n_jobs;
-    int64_t max_tiles = 0;
-    size_t stride = 0;
-    for (int i = 0; i < n_jobs; i++) {
-        size_t b = scan_scratch_bytes(jobs[i].n);
-        if (b > stride) stride = b;
-    }
-    stride = (stride + 255) & ~size_t(255);
+    p.err = &st->flags;
+    int64_t max_tiles = 1;
+    unsigned long long *cur = ws.buf + (int64_t)ws.cur * kMaxScanJobs * ws.job_words;
     for (int i = 0; i < n_jobs; i++) {
         p.job[i] = jobs[i];
-        p.partials[i] = (int64_t *)((char *)scratch + stride * i);
-        int64_t t = (jobs[i].n + kTile - 1) / kTile;
+        p.tiles[i] = cur + (int64_t)i * ws.job_words;
+        const int64_t t = (jobs[i].n + kTile - 1) / kTile;
         if (t > max_tiles) max_tiles = t;
     }
-    if (max_tiles > 0) {
-        dim3 grid((unsigned)max_tiles, n_jobs);
-        Launch L("k_scan_reduce", s);
-        k_scan_reduce<<<grid, kThreads, 0, s>>>(p);
-    }
+    p.next = ws.buf + (int64_t)(ws.cur ^ 1) * kMaxScanJobs * ws.job_words;
+    p.next_words = (int64_t)kMaxScanJobs * ws.job_words;
+    if (ws.used && ws.last != s) cudaStreamWaitEvent(s, ws.done, 0);
+    dim3 grid((unsigned)max_tiles, n_jobs);
     {
-        Launch L("k_scan_partials", s);
-        k_scan_partials<<<n_jobs, 1024, 0, s>>>(p);
+        Launch L("k_scan", s);
+        k_scan<<<grid, kThreads, 0, s>>>(p);
     }
-    if (max_tiles > 0) {
-        dim3 grid((unsigned)max_tiles, n_jobs);
-        Launch L("k_scan_down", s);
-        k_scan_down<<<grid, kThreads, 0, s>>>(p);
-    }
+    cudaEventRecord(ws.done, s);
+    ws.last = s;
+    ws.used = true;
+    ws.cur ^= 1;
 }
 
 }  // namespace tg

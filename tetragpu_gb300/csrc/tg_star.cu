@@ -1041,10 +1041,16 @@ k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int w
 // the 4T cell slots; the key's rank is the vertex's position.
 __global__ void __launch_bounds__(256)
 k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__restrict__ vkey,
-               const uint2 *__restrict__ vrank, int *__restrict__ vorder, int *__restrict__ dcount)
+               const uint2 *__restrict__ vrank, int64_t nwk, int *__restrict__ vorder,
+               int *__restrict__ dcount)
 {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
+    // the positions past the vertices with cells (their rows are empty)
+    if (v >= (int64_t)__ldg(&vrank[nwk].y)) {
+        vorder[v] = 0;
+        dcount[v] = 0;
+    }
     const int D = (int)(vt_off[v + 1] - vt_off[v]);
     if (D == 0) return;
     const long long key = vkey[v];
@@ -1175,12 +1181,13 @@ void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int6
 
 
 void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
-                         const uint2 *vrank, int32_t *vorder, int32_t *dcount, cudaStream_t s)
+                         const uint2 *vrank, int64_t nwk, int32_t *vorder, int32_t *dcount,
+                         cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_vorder_place", s);
-    k_vorder_place<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vt_off, V, vkey, vrank, vorder,
-                                                                dcount);
+    k_vorder_place<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vt_off, V, vkey, vrank, nwk,
+                                                                vorder, dcount);
 }
 
 void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
