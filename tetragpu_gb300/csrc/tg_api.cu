@@ -460,10 +460,10 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
         // id-ordered passes over the occurrence slots
         if (et_off || ef_off || ee_off || ev) {
-            char *scratch2;
-            TRY(tmp.alloc(&scratch2, (int64_t)edge_offsets_scratch_bytes(6 * T, E) + 256));
+            uint32_t *len;
+            TRY(tmp.alloc(&len, E));
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
-                                ev, scratch2, s);
+                                ev, len, m->scan, m->st, s);
         }
         if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, s);
         // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
@@ -666,7 +666,8 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
         src = reinterpret_cast<const int32_t *>(m->tvs);
     }
     // the scan workspace of every later scan on the mesh, zeroed once
-    m->scan.job_words = scan_job_words(std::max(std::max(V, T), (6 * T + 31) / 32));
+    m->scan.job_words = std::max(scan_job_words(std::max(std::max(V, T), (6 * T + 31) / 32)),
+                                 (edge_offsets_words(6 * T) + kMaxScanJobs - 1) / kMaxScanJobs);
     const size_t ws_bytes = (size_t)2 * kMaxScanJobs * m->scan.job_words * 8;
     CK(cudaMallocAsync((void **)&m->scan.buf, ws_bytes, s));
     CK(cudaMemsetAsync(m->scan.buf, 0, ws_bytes, s));

@@ -67,6 +67,62 @@ struct ScanWorkspace {
 };
 int64_t scan_job_words(int64_t max_n);
 void scan_batch(const ScanJob *jobs, int n_jobs, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
+// For another single-pass kernel on the workspace: the buffer to use now
+// (kMaxScanJobs * job_words words, zero), the one to zero for the next user;
+// scan_ws_end after the launch.
+void scan_ws_begin(ScanWorkspace &ws, cudaStream_t s, unsigned long long **cur,
+                   unsigned long long **next, int64_t *next_words);
+void scan_ws_end(ScanWorkspace &ws, cudaStream_t s);
+
+#ifdef __CUDACC__
+// Single-pass scan step (decoupled look-back, Merrill and Garland), called by
+// one whole warp: publish tile `tile`'s sum in w[tile] (sum << 2 | 1), add
+// the published sums of the tiles before it, 32 at a time (lane i reads the
+// i-th tile back), until one holds an inclusive prefix (sum << 2 | 2); then
+// publish its own inclusive prefix.  Returns the sum of the tiles before it
+// (in every lane).  Tiles are numbered in block start order, so the tiles
+// waited for are running; after kLookbackPolls polls the wait gives up and
+// sets ST_SCAN_STALLED.
+constexpr unsigned kLookbackPolls = 1u << 16;
+__device__ __forceinline__ long long look_back(unsigned long long *w, long long tile, long long sum,
+                                               unsigned *err)
+{
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) atomicExch(w, ((unsigned long long)sum << 2) | 2ull);
+        return 0;
+    }
+    if (lane == 0) atomicExch(w + tile, ((unsigned long long)sum << 2) | 1ull);
+    long long prefix = 0;
+    long long k = tile - 1;   // the window: tiles k - 31 .. k
+    unsigned polls = 0;
+    while (true) {
+        const long long t = k - lane;
+        const unsigned long long x =
+            t >= 0 ? *reinterpret_cast<volatile unsigned long long *>(w + t) : 0ull;
+        const unsigned f = (unsigned)(x & 3ull);
+        const unsigned pre = __ballot_sync(0xffffffffu, f == 2);
+        const int first = pre ? __ffs(pre) - 1 : 31;   // nearest inclusive prefix, or all
+        const unsigned need = first >= 31 ? 0xffffffffu : (2u << first) - 1u;
+        if (__ballot_sync(0xffffffffu, f == 0) & need) {   // a tile has not published yet
+            if (++polls > kLookbackPolls) {
+                if (lane == 0) atomicOr(err, ST_SCAN_STALLED);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        long long v = lane <= first ? (long long)(x >> 2) : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        prefix += v;
+        if (pre) break;
+        k -= 32;
+    }
+    if (lane == 0) atomicExch(w + tile, ((unsigned long long)(prefix + sum) << 2) | 2ull);
+    return prefix;
+}
+#endif
 
 // ---- pipeline kernels (tg_kernels.cu) ----
 struct Sizes {
@@ -150,12 +206,14 @@ void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const
                       int64_t *seg_ef, cudaStream_t s);
 
 // ET / EF / EE offsets in edge-id order from one scan over the 6T edge slots
-size_t edge_offsets_scratch_bytes(int64_t n_slots, int64_t E);
-// (also writes EV when ev is given)
+// ET/EF/EE offsets in edge-id order in one pass (also EV when ev is given;
+// len: E scratch words); edge_offsets_words = the tile words it needs in the
+// scan workspace
+int64_t edge_offsets_words(int64_t n_slots);
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
-                         void *scratch, cudaStream_t s);
+                         uint32_t *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
 // FV, FT[f][0] and FF offsets in face-id order (nw = words of the face bitmap)
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
                        const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,

@@ -19,8 +19,6 @@ constexpr int kThreads = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;  // 2048 elements per tile
 
-constexpr unsigned kLookbackPolls = 1u << 16;
-
 struct ScanParams {
     ScanJob job[kMaxScanJobs];
     // per array: one word per tile (sum << 2 | 1 once the tile's sum is
@@ -81,37 +79,6 @@ __device__ __forceinline__ int64_t block_exclusive_scan(int64_t x, int64_t &excl
     return total;
 }
 
-// Publish tile `tile`'s sum and return the sum of the tiles before it.
-__device__ __forceinline__ int64_t look_back(unsigned long long *w, int64_t tile, int64_t sum,
-                                             unsigned *err)
-{
-    if (tile == 0) {
-        atomicExch(w, ((unsigned long long)sum << 2) | 2ull);
-        return 0;
-    }
-    atomicExch(w + tile, ((unsigned long long)sum << 2) | 1ull);
-    int64_t prefix = 0;
-    int64_t k = tile - 1;
-    unsigned polls = 0;
-    while (true) {
-        const unsigned long long x = *reinterpret_cast<volatile unsigned long long *>(w + k);
-        const unsigned f = (unsigned)(x & 3ull);
-        if (f == 0) {   // tile k's block has not published yet
-            if (++polls > kLookbackPolls) {
-                atomicOr(err, ST_SCAN_STALLED);
-                break;
-            }
-            __nanosleep(32);
-            continue;
-        }
-        prefix += (int64_t)(x >> 2);
-        if (f == 2) break;   // an inclusive prefix: done (tile 0 always has one)
-        --k;
-    }
-    atomicExch(w + tile, ((unsigned long long)(prefix + sum) << 2) | 2ull);
-    return prefix;
-}
-
 __global__ void __launch_bounds__(kThreads) k_scan(ScanParams p)
 {
     const int jb = blockIdx.y;
@@ -144,7 +111,10 @@ __global__ void __launch_bounds__(kThreads) k_scan(ScanParams p)
     }
     int64_t excl;
     const int64_t total = block_exclusive_scan<kThreads>(s, excl, sm);
-    if (threadIdx.x == 0) s_prefix = look_back(w, tile, total, p.err);
+    if (threadIdx.x < 32) {   // warp 0
+        const int64_t pre = look_back(w, tile, total, p.err);
+        if (threadIdx.x == 0) s_prefix = pre;
+    }
     __syncthreads();
     int64_t run = s_prefix + excl;
 #pragma unroll
@@ -169,21 +139,34 @@ void scan_batch(const ScanJob *jobs, int n_jobs, ScanWorkspace &ws, DevStatus *s
     p.n_jobs = n_jobs;
     p.err = &st->flags;
     int64_t max_tiles = 1;
-    unsigned long long *cur = ws.buf + (int64_t)ws.cur * kMaxScanJobs * ws.job_words;
+    unsigned long long *cur;
+    scan_ws_begin(ws, s, &cur, &p.next, &p.next_words);
     for (int i = 0; i < n_jobs; i++) {
         p.job[i] = jobs[i];
         p.tiles[i] = cur + (int64_t)i * ws.job_words;
         const int64_t t = (jobs[i].n + kTile - 1) / kTile;
         if (t > max_tiles) max_tiles = t;
     }
-    p.next = ws.buf + (int64_t)(ws.cur ^ 1) * kMaxScanJobs * ws.job_words;
-    p.next_words = (int64_t)kMaxScanJobs * ws.job_words;
-    if (ws.used && ws.last != s) cudaStreamWaitEvent(s, ws.done, 0);
     dim3 grid((unsigned)max_tiles, n_jobs);
     {
         Launch L("k_scan", s);
         k_scan<<<grid, kThreads, 0, s>>>(p);
     }
+    scan_ws_end(ws, s);
+}
+
+void scan_ws_begin(ScanWorkspace &ws, cudaStream_t s, unsigned long long **cur,
+                   unsigned long long **next, int64_t *next_words)
+{
+    const int64_t words = (int64_t)kMaxScanJobs * ws.job_words;
+    *cur = ws.buf + (int64_t)ws.cur * words;
+    *next = ws.buf + (int64_t)(ws.cur ^ 1) * words;
+    *next_words = words;
+    if (ws.used && ws.last != s) cudaStreamWaitEvent(s, ws.done, 0);
+}
+
+void scan_ws_end(ScanWorkspace &ws, cudaStream_t s)
+{
     cudaEventRecord(ws.done, s);
     ws.last = s;
     ws.used = true;

@@ -824,10 +824,10 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
 // occurrences, so scanning the 6T edge-occurrence slots in order visits the
 // edges in id order: a slot holding a first occurrence contributes the ET
 // and EF row lengths k_star_a left there and deg(a) + deg(b) - 2 for EE.
-// The reduce pass visits a tile's slots, records every edge's three lengths
-// (one packed word per edge id) and EV, and sums them per tile; the down pass
-// scans the packed words of the same tile's id range (ids are contiguous
-// over a slot range), so it gathers nothing.
+// One pass: a block takes a tile of slots (in start order), gathers each of
+// its edges' row lengths (packed in one word by id) and EV, scans the three
+// sums with a look-back over the tiles before it, then writes the offsets of
+// its edges from the packed words it just wrote.
 #ifndef TG_EDGE_ITEMS
 #define TG_EDGE_ITEMS 8
 #endif
@@ -842,8 +842,11 @@ struct EdgeOffsets {
     const int4 *tvs;
     const int32_t *deg;
     const uint2 *erank;
-    int64_t n_slots;
-    int64_t *partials;   // 3 per tile
+    int64_t n_slots, n_tiles;
+    unsigned long long *tiles;   // 3 * n_tiles tile words (ET, EF, EE), then the ticket
+    unsigned long long *next;    // the workspace buffer zeroed for the next user
+    int64_t next_words;
+    unsigned *err;
     uint32_t *len;       // [E]: ET | EF << 8 | EE << 16
     int64_t *et_off, *ef_off, *ee_off;
     int32_t *ev;         // [2E] or null: the edge's two vertices, ascending
@@ -900,107 +903,77 @@ __device__ __forceinline__ uint32_t slot_bits(const EdgeOffsets &p, long long s0
     return kEdgeItems == 32 ? w : (w >> (s0 & 31)) & ((1u << kEdgeItems) - 1u);
 }
 
-__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_reduce(EdgeOffsets p)
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets(EdgeOffsets p)
 {
-    const long long s0 = (long long)blockIdx.x * kEdgeTile + threadIdx.x * kEdgeItems;
+    {
+        const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.next_words;
+             i += nthreads)
+            p.next[i] = 0ull;
+    }
+    __shared__ long long s_tile, s_pre[3];
+    if (threadIdx.x == 0) s_tile = (long long)atomicAdd(p.tiles + 3 * p.n_tiles, 1ull);
+    __syncthreads();
+    const long long tile = s_tile;
+    if (p.n_tiles == 0) {   // no slots: the totals alone
+        if (tile == 0 && threadIdx.x == 0) {
+            if (p.et_off) p.et_off[p.E] = 0;
+            if (p.ef_off) p.ef_off[p.E] = 0;
+            if (p.ee_off) p.ee_off[p.E] = 0;
+        }
+        return;
+    }
+    if (tile >= p.n_tiles) return;
+    const long long s0 = tile * kEdgeTile + threadIdx.x * kEdgeItems;
     long long x[3] = {0, 0, 0};
     const uint32_t bits = slot_bits(p, s0);
-    if (bits) {
-        int id = rank_of(p.erank, s0);
-        for (uint32_t m = bits; m; m &= m - 1) {
-            const int i = __ffs(m) - 1;
-            const long long s = s0 + i;
-            if (s >= p.n_slots) break;
-            const long long cell = s / 6;
-            const int j = (int)(s - 6 * cell);
-            const int4 w = __ldg(p.tvs + cell);
-            const int a = get4(w, j < 3 ? 0 : (j < 5 ? 1 : 2));
-            const int b = get4(w, j < 3 ? j + 1 : (j == 3 ? 2 : 3));
-            const unsigned short c = p.ecnt[s];
-            const int et = c & 0xff, ef = c >> 8;
-            const int ee = p.ee_off ? __ldg(p.deg + a) + __ldg(p.deg + b) - 2 : 0;
-            x[0] += et;
-            x[1] += ef;
-            x[2] += ee;
-            p.len[id] = (uint32_t)c | ((uint32_t)ee << 16);
-            if (p.ev) reinterpret_cast<int2 *>(p.ev)[id] = make_int2(a, b);
-            id++;
-        }
+    const int id0 = bits ? rank_of(p.erank, s0) : 0;
+    int id = id0;
+    for (uint32_t m = bits; m; m &= m - 1) {
+        const int i = __ffs(m) - 1;
+        const long long s = s0 + i;
+        if (s >= p.n_slots) break;
+        const long long cell = s / 6;
+        const int j = (int)(s - 6 * cell);
+        const int4 w = __ldg(p.tvs + cell);
+        const int a = get4(w, j < 3 ? 0 : (j < 5 ? 1 : 2));
+        const int b = get4(w, j < 3 ? j + 1 : (j == 3 ? 2 : 3));
+        const unsigned short c = p.ecnt[s];
+        const int et = c & 0xff, ef = c >> 8;
+        const int ee = p.ee_off ? __ldg(p.deg + a) + __ldg(p.deg + b) - 2 : 0;
+        x[0] += et;
+        x[1] += ef;
+        x[2] += ee;
+        p.len[id] = (uint32_t)c | ((uint32_t)ee << 16);
+        if (p.ev) reinterpret_cast<int2 *>(p.ev)[id] = make_int2(a, b);
+        id++;
     }
     long long excl[3], tot[3];
     block_scan3<kEdgeThreads>(x, excl, tot);
-    if (threadIdx.x == 0)
-        for (int q = 0; q < 3; q++) p.partials[3 * blockIdx.x + q] = tot[q];
-}
-
-__global__ void __launch_bounds__(1024) k_edge_offsets_partials(EdgeOffsets p, int64_t n_tiles)
-{
-    // one block, chunks of 4096 tiles: a thread loads four consecutive
-    // tiles' triples at once (twelve loads in flight), one block-wide scan
-    // of the thread sums per chunk
-    constexpr int kPer = 4;
-    long long carry[3] = {0, 0, 0};
-    for (long long b = 0; b < n_tiles; b += 1024 * kPer) {
-        const long long i0 = b + (long long)threadIdx.x * kPer;
-        long long v[kPer][3], x[3] = {0, 0, 0};
-#pragma unroll
-        for (int k = 0; k < kPer; k++)
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-                v[k][q] = i0 + k < n_tiles ? p.partials[3 * (i0 + k) + q] : 0;
-                x[q] += v[k][q];
-            }
-        long long run[3], tot[3];
-        block_scan3<1024>(x, run, tot);
-#pragma unroll
-        for (int k = 0; k < kPer; k++)
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-                if (i0 + k < n_tiles) p.partials[3 * (i0 + k) + q] = carry[q] + run[q];
-                run[q] += v[k][q];
-            }
-#pragma unroll
-        for (int q = 0; q < 3; q++) carry[q] += tot[q];
+    if (threadIdx.x < 96) {   // one look-back per sum, warps 0-2 at once
+        const int q = threadIdx.x >> 5;
+        const long long t = q == 0 ? tot[0] : (q == 1 ? tot[1] : tot[2]);
+        const long long pre = look_back(p.tiles + q * p.n_tiles, tile, t, p.err);
+        if ((threadIdx.x & 31) == 0) s_pre[q] = pre;
     }
-    if (threadIdx.x == 0) {
-        if (p.et_off) p.et_off[p.E] = carry[0];
-        if (p.ef_off) p.ef_off[p.E] = carry[1];
-        if (p.ee_off) p.ee_off[p.E] = carry[2];
-    }
-}
-
-__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets_down(EdgeOffsets p)
-{
-    // the tile's edges are the ids [lo, hi): a run of consecutive ones a
-    // thread (at most kEdgeItems)
-    const long long t0 = (long long)blockIdx.x * kEdgeTile;
-    const int lo = rank_of(p.erank, t0);
-    const int hi = rank_of(p.erank, min(t0 + kEdgeTile, (long long)p.n_slots));
-    const int per = (hi - lo + kEdgeThreads - 1) / kEdgeThreads;
-    const int i0 = lo + per * (int)threadIdx.x;
-    const int k_end = min(per, hi - i0);
-    // per-edge lengths fit 8 + 8 + 16 bits: a thread's sums fit 32 bits
-    int x0 = 0, x1 = 0, x2 = 0;
-    for (int k = 0; k < k_end; k++) {
-        const uint32_t w = p.len[i0 + k];
-        x0 += w & 0xff;
-        x1 += (w >> 8) & 0xff;
-        x2 += w >> 16;
-    }
-    long long x[3] = {x0, x1, x2}, excl[3], tot[3];
-    block_scan3<kEdgeThreads>(x, excl, tot);
+    __syncthreads();
     long long run[3];
-    for (int q = 0; q < 3; q++) run[q] = p.partials[3 * blockIdx.x + q] + excl[q];
-    // the words again (cache hits): keeping a run in registers would cost
-    // occupancy
-    for (int k = 0; k < k_end; k++) {
-        const uint32_t w = p.len[i0 + k];
-        if (p.et_off) p.et_off[i0 + k] = run[0];
-        if (p.ef_off) p.ef_off[i0 + k] = run[1];
-        if (p.ee_off) p.ee_off[i0 + k] = run[2];
+#pragma unroll
+    for (int q = 0; q < 3; q++) run[q] = s_pre[q] + excl[q];
+    // this thread's packed words again (it wrote them: cache hits)
+    for (int k = id0; k < id; k++) {
+        const uint32_t w = p.len[k];
+        if (p.et_off) p.et_off[k] = run[0];
+        if (p.ef_off) p.ef_off[k] = run[1];
+        if (p.ee_off) p.ee_off[k] = run[2];
         run[0] += w & 0xff;
         run[1] += (w >> 8) & 0xff;
         run[2] += w >> 16;
+    }
+    if (tile == p.n_tiles - 1 && threadIdx.x == 0) {
+        if (p.et_off) p.et_off[p.E] = s_pre[0] + tot[0];
+        if (p.ef_off) p.ef_off[p.E] = s_pre[1] + tot[1];
+        if (p.ee_off) p.ee_off[p.E] = s_pre[2] + tot[2];
     }
 }
 
@@ -1118,33 +1091,38 @@ void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int 
         win2 ? window_count(n_entries, win_size2) : 0, win_size2, win2);
 }
 
-size_t edge_offsets_scratch_bytes(int64_t n_slots, int64_t E)
+int64_t edge_offsets_words(int64_t n_slots)
 {
-    return (size_t)(3 * (n_slots / kEdgeTile + 2)) * sizeof(int64_t) + (size_t)E * sizeof(uint32_t);
+    return 3 * ((n_slots + kEdgeTile - 1) / kEdgeTile) + 1;
 }
 
 void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
-                         void *scratch, cudaStream_t s)
+                         uint32_t *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s)
 {
     const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
-    int64_t *partials = (int64_t *)scratch;
-    uint32_t *len = reinterpret_cast<uint32_t *>(partials + 3 * (n_slots / kEdgeTile + 2));
-    EdgeOffsets p{eflag, reinterpret_cast<const unsigned short *>(ecnt), tvs, deg, erank, n_slots,
-                  partials, len, et_off, ef_off, ee_off, ev, E};
-    if (tiles > 0) {
-        Launch L("k_edge_offsets_reduce", s);
-        k_edge_offsets_reduce<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p);
-    }
+    EdgeOffsets p{};
+    p.eflag = eflag;
+    p.ecnt = reinterpret_cast<const unsigned short *>(ecnt);
+    p.tvs = tvs;
+    p.deg = deg;
+    p.erank = erank;
+    p.n_slots = n_slots;
+    p.n_tiles = tiles;
+    p.err = &st->flags;
+    p.len = len;
+    p.et_off = et_off;
+    p.ef_off = ef_off;
+    p.ee_off = ee_off;
+    p.ev = ev;
+    p.E = E;
+    scan_ws_begin(ws, s, &p.tiles, &p.next, &p.next_words);
     {
-        Launch L("k_edge_offsets_partials", s);
-        k_edge_offsets_partials<<<1, 1024, 0, s>>>(p, tiles);
+        Launch L("k_edge_offsets", s);
+        k_edge_offsets<<<(unsigned)std::max<int64_t>(tiles, 1), kEdgeThreads, 0, s>>>(p);
     }
-    if (tiles > 0) {
-        Launch L("k_edge_offsets_down", s);
-        k_edge_offsets_down<<<(unsigned)tiles, kEdgeThreads, 0, s>>>(p);
-    }
+    scan_ws_end(ws, s);
 }
 
 void launch_star_a(const StarA &a, cudaStream_t s)
