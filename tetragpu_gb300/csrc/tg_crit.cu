@@ -40,6 +40,54 @@ constexpr int kAdjWin = TG_ADJ_WIN;
 constexpr int kAdjCap = kAdjWin + kMaxDeg;
 constexpr int kAdjThreads = TG_ADJ_THREADS;
 
+// u's row (urow, un entries; read four at a time from 16-byte boundaries
+// when the array is aligned: i from i0 = -(ub mod 4), one load instruction
+// per four entries; else one entry at a time) against v's row (row, d
+// entries, shared memory): each w found at position lo of v's row sets bit lo
+// of bits_v and bit i of bits_u; pv = v's place in u's row.  The search is
+// branch-free with a fixed number of steps (TOP, TOP/2, .. 1; TOP the highest
+// power of 2 the row length can need; the first step only for rows longer
+// than TOP), so the lanes of a warp stay together.
+template <typename M, int TOP>
+__device__ __forceinline__ void adj_scan(const int *row, int d, const int *__restrict__ urow,
+                                         int i0, int un, int lim, bool vec, int v, M &bits_v,
+                                         M &bits_u, int &pv)
+{
+    for (; i0 < un; i0 += 4) {
+        int q[4];
+        if (vec && i0 + 4 <= lim) {
+            const int4 x = __ldg(reinterpret_cast<const int4 *>(urow + i0));
+            q[0] = x.x;
+            q[1] = x.y;
+            q[2] = x.z;
+            q[3] = x.w;
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; t++) q[t] = i0 + t < lim ? __ldg(urow + i0 + t) : 0;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int i = i0 + t;
+            if (i < 0 || i >= un) continue;
+            const int w = q[t];
+            if (w == v) {
+                pv = i;
+                continue;
+            }
+            // entries of v's row below w; the largest step only for a row
+            // that can need it (rows of up to TOP entries take one step less)
+            int lo = d > TOP && row[TOP - 1] < w ? TOP : 0;
+#pragma unroll
+            for (int step = TOP / 2; step > 0; step >>= 1)
+                if (lo + step <= d && row[lo + step - 1] < w) lo += step;
+            if (lo < d && row[lo] == w) {
+                bits_v |= (M)1 << lo;
+                bits_u |= (M)1 << i;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
            const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
@@ -85,56 +133,31 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
         if ((meta[e] >> 16) <= kMaxDeg && nb[e] > vid[e]) own[atomicAdd(&n_own, 1)] = e;
     __syncthreads();
     const int no = n_own;
+    const bool vec = (reinterpret_cast<uintptr_t>(vv) & 15) == 0;
     for (int k = threadIdx.x; k < no; k += blockDim.x) {
         const int e = own[k];
         const int m = meta[e], rs = m & 0xffff, d = m >> 16;
-        const int *row = nb + rs;
         const int v = vid[e], u = nb[e];
-        const bool vec = (reinterpret_cast<uintptr_t>(vv) & 15) == 0;
         const int64_t ub = vv_off[u];
         const int un = (int)(vv_off[u + 1] - ub);
         if (un > kMaxDeg) continue;  // u's own block reports it
-        unsigned long long bits_v = 0ull, bits_u = 0ull;
+        // entries of u's row at or past the array's end are not loaded
+        const int lim = (int)min(n_vv - ub, (int64_t)INT_MAX);
         int pv = -1;
-        // u's row read four entries at a time from 16-byte boundaries (one
-        // load instruction per four entries; the rows of a warp's lanes lie
-        // apart, so each load costs a memory transaction per lane), scalar
-        // loads for a last group that would end past the array, or when the
-        // caller's VV array itself is not 16-byte aligned
-        for (int64_t a0 = ub & ~3LL; a0 < ub + un; a0 += 4) {
-            int q[4];
-            if (vec && a0 + 4 <= n_vv) {
-                const int4 x = __ldg(reinterpret_cast<const int4 *>(vv + a0));
-                q[0] = x.x;
-                q[1] = x.y;
-                q[2] = x.z;
-                q[3] = x.w;
-            } else {
-#pragma unroll
-                for (int t = 0; t < 4; t++) q[t] = a0 + t < n_vv ? __ldg(vv + a0 + t) : 0;
-            }
-#pragma unroll
-            for (int t = 0; t < 4; t++) {
-                const int i = (int)(a0 + t - ub);
-                if (i < 0 || i >= un) continue;
-                const int w = q[t];
-                if (w == v) {
-                    pv = i;
-                    continue;
-                }
-                int lo = 0, hi = d;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (row[mid] < w) lo = mid + 1; else hi = mid;
-                }
-                if (lo < d && row[lo] == w) {
-                    bits_v |= 1ull << lo;
-                    bits_u |= 1ull << i;
-                }
-            }
+        unsigned long long bv, bu;
+        if (d <= 32 && un <= 32) {   // both masks fit 32 bits (the common case)
+            unsigned bv32 = 0u, bu32 = 0u;
+            adj_scan<unsigned, 16>(nb + rs, d, vv + ub, vec ? -(int)(ub & 3) : 0, un, lim, vec, v,
+                                   bv32, bu32, pv);
+            bv = bv32;
+            bu = bu32;
+        } else {
+            bv = bu = 0ull;
+            adj_scan<unsigned long long, 32>(nb + rs, d, vv + ub, vec ? -(int)(ub & 3) : 0, un,
+                                             lim, vec, v, bv, bu, pv);
         }
-        adj[base + e] = bits_v;
-        if (pv >= 0) adj[ub + pv] = bits_u;
+        adj[base + e] = bv;
+        if (pv >= 0) adj[ub + pv] = bu;
     }
 }
 
