@@ -233,3 +233,39 @@ def test_relations_copied_at_once_with_int32_offsets(gpu_lib):
             else:
                 assert np.array_equal(off.astype(np.int64), want[0]), name
                 assert np.array_equal(ent[:d["n_entries"]], want[1]), name
+
+
+def _ring(k, offset=0, rng=None):
+    # k cells around the axis (v, c): cells (v, c, r_i, r_i+1), ring closed.
+    # v and c lie in k cells with k + 1 neighbours each, the ring vertices in
+    # two cells with four neighbours.  Vertex ids permuted when rng is given.
+    v, c = 0, 1
+    tv = np.array([[v, c, 2 + i, 2 + (i + 1) % k] for i in range(k)], np.int64)
+    n = k + 2
+    if rng is not None:
+        perm = rng.permutation(n)
+        tv = perm[tv]
+        tv = rng.permuted(tv, axis=1)   # slots unsorted too
+    return (tv + offset).astype(np.int32), n
+
+
+@pytest.mark.parametrize("k", [33, 40, 63])
+def test_wide_stars_and_long_rows(gpu_lib, oracle, k):
+    """Stars of more than 32 cells and VV rows of more than 32 neighbours take
+    the 64-bit star-position and link masks (narrower windows of the same
+    mesh the 32-bit ones): every relation and the classes against the oracle,
+    alone and next to a coned grid in one mesh."""
+    rng = np.random.default_rng(k)
+    tv, n = _ring(k, rng=rng)
+    m = meshgen.Mesh(tv=tv, n_verts=n, coords=np.zeros((n, 3), np.float32), name=f"ring{k}")
+    _check_mesh(gpu_lib, oracle, m)
+    grid = meshgen.kuhn_mesh(3, 0.4, seed=k)
+    tv2 = np.concatenate([grid.tv, tv + grid.n_verts])
+    both = meshgen.Mesh(tv=tv2, n_verts=grid.n_verts + n,
+                        coords=np.zeros((grid.n_verts + n, 3), np.float32), name="grid+ring")
+    _check_mesh(gpu_lib, oracle, both)
+    field = rng.standard_normal(both.n_verts).astype(np.float32)
+    tvs = oracle.canonicalize(both.tv, both.n_verts)
+    with gpu_lib.Mesh(both.tv, both.n_verts) as g:
+        assert np.array_equal(g.critical_points(field),
+                              oracle.critical_points(tvs, both.n_verts, field))
