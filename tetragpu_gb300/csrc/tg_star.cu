@@ -1036,7 +1036,14 @@ k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__r
 // VT rows copied into processing order: a warp fetches 32 rows' positions
 // and sources at once, then copies them one after another, lanes across the
 // row
-__global__ void __launch_bounds__(256, 8)
+#ifndef TG_VTP_ROWS
+#define TG_VTP_ROWS 8
+#endif
+#ifndef TG_VTP_MINB
+#define TG_VTP_MINB 4
+#endif
+constexpr int kVtpRows = TG_VTP_ROWS;
+__global__ void __launch_bounds__(256, TG_VTP_MINB)
 k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int64_t V,
            const int64_t *__restrict__ vt_off, const int *__restrict__ vt, int *__restrict__ vtp)
 {
@@ -1051,11 +1058,24 @@ k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int
         D = (int)(pofs[r + 1] - dst);
         if (D > 0) src = __ldg(vt_off + __ldg(vorder + r));
     }
-    for (int j = 0; j < 32; j++) {
-        const int Dj = __shfl_sync(0xffffffffu, D, j);
-        const long long dj = __shfl_sync(0xffffffffu, dst, j);
-        const long long sj = __shfl_sync(0xffffffffu, src, j);
-        for (int k = lane; k < Dj; k += 32) vtp[dj + k] = __ldg(vt + sj + k);
+    // kVtpRows rows at a time: their loads are in flight together (lane k
+    // takes entry k; entries past 32 of a longer row follow)
+    constexpr int R = kVtpRows;
+    for (int j = 0; j < 32; j += R) {
+        int x[R], Dj[R];
+        long long dj[R], sj[R];
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            Dj[t] = __shfl_sync(0xffffffffu, D, j + t);
+            dj[t] = __shfl_sync(0xffffffffu, dst, j + t);
+            sj[t] = __shfl_sync(0xffffffffu, src, j + t);
+            x[t] = lane < Dj[t] ? __ldg(vt + sj[t] + lane) : 0;
+        }
+#pragma unroll
+        for (int t = 0; t < R; t++) {
+            if (lane < Dj[t]) vtp[dj[t] + lane] = x[t];
+            for (int k = lane + 32; k < Dj[t]; k += 32) vtp[dj[t] + k] = __ldg(vt + sj[t] + k);
+        }
     }
 }
 
