@@ -53,18 +53,21 @@ __device__ __forceinline__ void adj_scan(const int *row, int d, const int *__res
                                          int i0, int un, int lim, bool vec, int v, M &bits_v,
                                          M &bits_u, int &pv)
 {
+    // the next four entries are loaded while the current four are searched
+    auto load4 = [&](int j) -> int4 {
+        if (vec && j + 4 <= lim) return __ldg(reinterpret_cast<const int4 *>(urow + j));
+        int4 x;
+        x.x = j < lim && j < un ? __ldg(urow + j) : 0;
+        x.y = j + 1 < lim && j + 1 < un ? __ldg(urow + j + 1) : 0;
+        x.z = j + 2 < lim && j + 2 < un ? __ldg(urow + j + 2) : 0;
+        x.w = j + 3 < lim && j + 3 < un ? __ldg(urow + j + 3) : 0;
+        return x;
+    };
+    int4 nxt = i0 < un ? load4(i0) : make_int4(0, 0, 0, 0);
     for (; i0 < un; i0 += 4) {
-        int q[4];
-        if (vec && i0 + 4 <= lim) {
-            const int4 x = __ldg(reinterpret_cast<const int4 *>(urow + i0));
-            q[0] = x.x;
-            q[1] = x.y;
-            q[2] = x.z;
-            q[3] = x.w;
-        } else {
-#pragma unroll
-            for (int t = 0; t < 4; t++) q[t] = i0 + t < lim ? __ldg(urow + i0 + t) : 0;
-        }
+        const int4 cur = nxt;
+        if (i0 + 4 < un) nxt = load4(i0 + 4);
+        const int q[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             const int i = i0 + t;
