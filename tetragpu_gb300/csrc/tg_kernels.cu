@@ -411,9 +411,10 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
     constexpr int G = kEeGroup;
     const int g = lane / G, gl = lane % G;
     const int n_small = __popc(small);
+    const bool all_small = small == 0xffffffffu;   // no lanes to skip (the common case)
     for (int k = 0; k < n_small; k += 32 / G) {
         const int which = k + g;
-        const int src = which < n_small ? (int)__fns(small, 0, which + 1) : 0;
+        const int src = all_small ? which : (which < n_small ? (int)__fns(small, 0, which + 1) : 0);
         const int64_t ra = __shfl_sync(kFull, my_ra, src), rb = __shfl_sync(kFull, my_rb, src);
         int na = __shfl_sync(kFull, my_na, src), nb = __shfl_sync(kFull, my_nb, src);
         const int64_t o = __shfl_sync(kFull, my_out, src);
