@@ -25,6 +25,7 @@ __global__ void __launch_bounds__(256)
 k_batch_shift(const int4 *__restrict__ tv, int64_t T, const int64_t *__restrict__ seg_c,
               const int64_t *__restrict__ seg_v, int64_t n, int4 *__restrict__ out)
 {
+    griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     int64_t lo = 0, hi = n;  // last i with seg_c[i] <= c
@@ -45,6 +46,7 @@ k_batch_shift(const int4 *__restrict__ tv, int64_t T, const int64_t *__restrict_
 __global__ void __launch_bounds__(256)
 k_rebase32(const int *__restrict__ src, int64_t n, int shift, int *__restrict__ dst)
 {
+    griddep_wait();
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int x = src[k];
@@ -54,6 +56,7 @@ k_rebase32(const int *__restrict__ src, int64_t n, int shift, int *__restrict__ 
 __global__ void __launch_bounds__(256)
 k_rebase64(const int64_t *__restrict__ src, int64_t n, int64_t shift, int64_t *__restrict__ dst)
 {
+    griddep_wait();
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     dst[k] = src[k] - shift;
@@ -193,7 +196,7 @@ tg_status tg_batch_create(const int32_t *tv, const int64_t *n_cells, const int64
                                 cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) {
             Launch L("k_batch_shift", s);
-            k_batch_shift<<<blocks(T), 256, 0, s>>>(d_in, T, d_seg, d_seg + n_meshes + 1,
+            launch_pdl(k_batch_shift, blocks(T), 256, 0, s, d_in, T, d_seg, d_seg + n_meshes + 1,
                                                     n_meshes, d_tv);
             e = cudaGetLastError();
         }
@@ -339,7 +342,7 @@ tg_status tg_batch_copy_relation(tg_batch *b, int64_t i, int r, int64_t *off_hos
         e = cudaMallocAsync(&d_ent, (size_t)n_ent * 4, s);
         if (e == cudaSuccess) {
             Launch L("k_rebase32", s);
-            k_rebase32<<<blocks(n_ent), 256, 0, s>>>(ent + e_lo, n_ent, (int)shift, d_ent);
+            launch_pdl(k_rebase32, blocks(n_ent), 256, 0, s, ent + e_lo, n_ent, (int)shift, d_ent);
             e = cudaMemcpyAsync(ent_host, d_ent, (size_t)n_ent * 4, cudaMemcpyDeviceToHost, s);
         }
     }
@@ -347,7 +350,7 @@ tg_status tg_batch_copy_relation(tg_batch *b, int64_t i, int r, int64_t *off_hos
         e = cudaMallocAsync(&d_off, (size_t)n_off * 8, s);
         if (e == cudaSuccess) {
             Launch L("k_rebase64", s);
-            k_rebase64<<<blocks(n_off), 256, 0, s>>>(off + r0, n_off, e_lo, d_off);
+            launch_pdl(k_rebase64, blocks(n_off), 256, 0, s, off + r0, n_off, e_lo, d_off);
             e = cudaMemcpyAsync(off_host, d_off, (size_t)n_off * 8, cudaMemcpyDeviceToHost, s);
         }
     }

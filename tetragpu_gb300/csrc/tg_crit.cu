@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
            const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
 {
+    griddep_wait();
     __shared__ int nb[kAdjCap];
     __shared__ int meta[kAdjCap];   // row start | row length << 16
     __shared__ int vid[kAdjCap];
@@ -177,6 +178,7 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
                 const unsigned long long *__restrict__ adj, const F *__restrict__ field_v0,
                 int64_t v0, int64_t nv, unsigned *__restrict__ classes3_v0)
 {
+    griddep_wait();
     // rows [v0, v0 + nv); field and classes indexed from v0 (a vertex range
     // holds every neighbour of its vertices when it is a whole mesh of a batch)
     const int64_t v = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,7 +234,7 @@ void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
-    k_crit_adj<<<(unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s>>>(
+    launch_pdl(k_crit_adj, (unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s,
         vv_off, vv, n_vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
 }
 
@@ -245,10 +247,10 @@ void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64
     const auto *a = reinterpret_cast<const unsigned long long *>(adj);
     Launch L("k_crit_classify", s);
     if (field_type == 1)
-        k_crit_classify<double><<<grid, kClassifyThreads, 0, s>>>(
+        launch_pdl(k_crit_classify<double>, grid, kClassifyThreads, 0, s,
             vv_off, vv, a, (const double *)field, v0, nv, classes3);
     else
-        k_crit_classify<float><<<grid, kClassifyThreads, 0, s>>>(
+        launch_pdl(k_crit_classify<float>, grid, kClassifyThreads, 0, s,
             vv_off, vv, a, (const float *)field, v0, nv, classes3);
 }
 

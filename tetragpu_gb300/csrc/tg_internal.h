@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <utility>
 
 #include "tetragpu.h"
 
@@ -290,6 +291,33 @@ void prof_end(const char *name, cudaStream_t s);
 
 // RAII wrapper around every launch: counts it and, when the kernel is the
 // one selected with tg_profile_kernel, brackets it with CUDA events.
+#ifdef __CUDACC__
+// Programmatic dependent launch.  Kernels go out with programmatic stream
+// serialisation allowed, so a kernel's launch is processed while the kernel
+// before it on the stream runs.  Every kernel starts with griddep_wait(),
+// which returns once the grids it depends on have completed and their memory
+// is visible (at once when it was not launched that way).  The kernels do not
+// signal their dependents early: blocks of the next kernel waiting on SMs
+// cost the running one more than the earlier start saves.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args &&...args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+#endif
+
 struct Launch {
     const char *name;
     cudaStream_t s;

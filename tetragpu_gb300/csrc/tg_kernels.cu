@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(256)
 k_canon(const int32_t *tv, int64_t T, int V, int4 *tvs, int *deg_t, int4 *occ, DevStatus *st,
         int aligned)
 {
+    griddep_wait();
     __shared__ int hkey[kCanonHash], hcnt[kCanonHash];
     for (int i = threadIdx.x; i < kCanonHash; i += blockDim.x) {
         hkey[i] = -1;
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(256)
 k_vt_fill(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__ vt_off,
           const int4 *__restrict__ occ, int *__restrict__ vt)
 {
+    griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     const int4 w = tvs[c];
@@ -162,6 +164,7 @@ k_vt_fill(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__ v
 __global__ void __launch_bounds__(256)
 k_sort_rows(const int64_t *__restrict__ off, int *__restrict__ ent, int64_t n_rows)
 {
+    griddep_wait();
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r < n_rows) {
         const int64_t b = off[r], e = off[r + 1];
@@ -195,6 +198,7 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__re
              int *__restrict__ fe, int64_t *__restrict__ tt_off, int *__restrict__ tt,
              int64_t *__restrict__ ff_off)
 {
+    griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     if (c == T - 1) {
@@ -245,6 +249,7 @@ __global__ void __launch_bounds__(256)
 k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
           const int64_t *__restrict__ ff_off, int *__restrict__ ff)
 {
+    griddep_wait();
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     // the faces of the face's two cells, f itself (once in each row) and a
@@ -391,6 +396,7 @@ __global__ void __launch_bounds__(kEeWarps * 32)
 k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_off,
           const int *__restrict__ eid, const int64_t *__restrict__ ee_off, int *__restrict__ ee)
 {
+    griddep_wait();
     const int lane = threadIdx.x & 31;
     const int64_t e0 = ((int64_t)blockIdx.x * kEeWarps + (threadIdx.x >> 5)) * 32;
     if (e0 >= E) return;  // warp-uniform
@@ -443,6 +449,7 @@ k_tt_vertex(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__
             const int *__restrict__ vt, int *__restrict__ cnt, const int64_t *__restrict__ tt_off,
             int *__restrict__ tt)
 {
+    griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     const int4 w = tvs[c];
@@ -476,6 +483,7 @@ k_tt_vertex(const int4 *__restrict__ tvs, int64_t T, const int64_t *__restrict__
 __global__ void __launch_bounds__(256)
 k_widen(const int *__restrict__ src, long long *__restrict__ dst, int64_t n)
 {
+    griddep_wait();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = src[i];
@@ -485,6 +493,7 @@ k_widen(const int *__restrict__ src, long long *__restrict__ dst, int64_t n)
 __global__ void __launch_bounds__(256)
 k_narrow(const int64_t *__restrict__ src, int *__restrict__ dst, int64_t n)
 {
+    griddep_wait();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = (int)src[i];
@@ -492,6 +501,7 @@ k_narrow(const int64_t *__restrict__ src, int *__restrict__ dst, int64_t n)
 
 __global__ void __launch_bounds__(256) k_narrow_multi(NarrowJobs j)
 {
+    griddep_wait();
     const int64_t total = j.start[j.n];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -507,6 +517,7 @@ __global__ void __launch_bounds__(256)
 k_pad_rows(const int64_t *__restrict__ off, const int *__restrict__ ent, int64_t rows, int width,
            long long *__restrict__ out, unsigned *__restrict__ counts)
 {
+    griddep_wait();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= rows * width) return;
     const int64_t r = i / width;
@@ -519,6 +530,7 @@ k_pad_rows(const int64_t *__restrict__ off, const int *__restrict__ ent, int64_t
 
 __global__ void k_reset_status(DevStatus *st)
 {
+    griddep_wait();
     st->flags = 0;
     st->bad_cell = INT_MAX;
     st->bad_vertex = INT_MAX;
@@ -541,7 +553,7 @@ void launch_widen(const int32_t *src, int64_t *dst, int64_t n, cudaStream_t s)
     if (n == 0) return;
     Launch L("k_widen", s);
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
-    k_widen<<<(unsigned)blocks, 256, 0, s>>>(src, reinterpret_cast<long long *>(dst), n);
+    launch_pdl(k_widen, (unsigned)blocks, 256, 0, s, src, reinterpret_cast<long long *>(dst), n);
 }
 
 void launch_narrow(const int64_t *src, int32_t *dst, int64_t n, cudaStream_t s)
@@ -549,7 +561,7 @@ void launch_narrow(const int64_t *src, int32_t *dst, int64_t n, cudaStream_t s)
     if (n == 0) return;
     Launch L("k_narrow", s);
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
-    k_narrow<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n);
+    launch_pdl(k_narrow, (unsigned)blocks, 256, 0, s, src, dst, n);
 }
 
 void launch_narrow_multi(const NarrowJobs &j, cudaStream_t s)
@@ -558,7 +570,7 @@ void launch_narrow_multi(const NarrowJobs &j, cudaStream_t s)
     if (n == 0) return;
     Launch L("k_narrow_multi", s);
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
-    k_narrow_multi<<<(unsigned)blocks, 256, 0, s>>>(j);
+    launch_pdl(k_narrow_multi, (unsigned)blocks, 256, 0, s, j);
 }
 
 void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int width,
@@ -566,7 +578,7 @@ void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int w
 {
     if (rows == 0 || width == 0) return;
     Launch L("k_pad_rows", s);
-    k_pad_rows<<<blocks_for(rows * width, 256), 256, 0, s>>>(off, ent, rows, width,
+    launch_pdl(k_pad_rows, blocks_for(rows * width, 256), 256, 0, s, off, ent, rows, width,
                                                             reinterpret_cast<long long *>(out), counts);
 }
 
@@ -574,6 +586,7 @@ void launch_pad_rows(const int64_t *off, const int32_t *ent, int64_t rows, int w
 // status for the next call on the mesh (the host has consumed it)
 __global__ void k_publish(PublishArgs a)
 {
+    griddep_wait();
     if (threadIdx.x != 0) return;
     *a.h_st = *a.st;
     for (int i = 0; i < a.n; i++)
@@ -589,13 +602,13 @@ __global__ void k_publish(PublishArgs a)
 void launch_publish(const PublishArgs &a, cudaStream_t s)
 {
     Launch L("k_publish", s);
-    k_publish<<<1, 32, 0, s>>>(a);
+    launch_pdl(k_publish, 1, 32, 0, s, a);
 }
 
 void launch_reset_status(DevStatus *st, cudaStream_t s)
 {
     Launch L("k_reset_status", s);
-    k_reset_status<<<1, 1, 0, s>>>(st);
+    launch_pdl(k_reset_status, 1, 1, 0, s, st);
 }
 
 void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t *deg_t,
@@ -605,7 +618,7 @@ void launch_canon(const int32_t *tv_in, int64_t T, int64_t V, int4 *tvs, int32_t
     const int aligned = ((uintptr_t)tv_in & 15) == 0;
     {
         Launch L("k_canon", s);
-        k_canon<<<blocks_for(T, 256), 256, 0, s>>>(tv_in, T, (int)V, tvs, deg_t, occ, st, aligned);
+        launch_pdl(k_canon, blocks_for(T, 256), 256, 0, s, tv_in, T, (int)V, tvs, deg_t, occ, st, aligned);
     }
 }
 
@@ -615,7 +628,7 @@ void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, const int
     if (T == 0) return;
     {
         Launch L("k_vt_fill", s);
-        k_vt_fill<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, vt_off, occ, vt);
+        launch_pdl(k_vt_fill, blocks_for(T, 256), 256, 0, s, tvs, T, vt_off, occ, vt);
     }
 }
 
@@ -624,7 +637,7 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
     if (n_rows == 0) return;
     {
         Launch L("k_sort_rows", s);
-        k_sort_rows<<<blocks_for(n_rows, 256), 256, 0, s>>>(off, ent, n_rows);
+        launch_pdl(k_sort_rows, blocks_for(n_rows, 256), 256, 0, s, off, ent, n_rows);
     }
 }
 
@@ -639,7 +652,7 @@ void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
     if (T == 0) return;
     {
         Launch L("k_cell_fe_tt", s);
-        k_cell_fe_tt<<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, F, te, tf, ft, brank, fe, tt_off,
+        launch_pdl(k_cell_fe_tt, blocks_for(T, 256), 256, 0, s, tvs, T, F, te, tf, ft, brank, fe, tt_off,
                                                          tt, ff_off);
     }
 }
@@ -650,7 +663,7 @@ void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64
     if (F == 0) return;
     {
         Launch L("k_ff_fill", s);
-        k_ff_fill<<<blocks_for(F, 256), 256, 0, s>>>(ft, tf, F, ff_off, ff);
+        launch_pdl(k_ff_fill, blocks_for(F, 256), 256, 0, s, ft, tf, F, ff_off, ff);
     }
 }
 
@@ -660,7 +673,7 @@ void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const i
     if (E == 0) return;
     {
         Launch L("k_ee_fill", s);
-        k_ee_fill<<<blocks_for((E + 31) / 32, kEeWarps), kEeWarps * 32, 0, s>>>(ev, E, vv_off, eid_sorted,
+        launch_pdl(k_ee_fill, blocks_for((E + 31) / 32, kEeWarps), kEeWarps * 32, 0, s, ev, E, vv_off, eid_sorted,
                                                                    ee_off, ee);
     }
 }
@@ -671,7 +684,7 @@ void launch_tt_vertex_count(const int4 *tvs, int64_t T, const int64_t *vt_off, c
     if (T == 0) return;
     {
         Launch L("k_tt_vertex", s);
-        k_tt_vertex<false><<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, vt_off, vt, cnt, nullptr, nullptr);
+        launch_pdl(k_tt_vertex<false>, blocks_for(T, 256), 256, 0, s, tvs, T, vt_off, vt, cnt, nullptr, nullptr);
     }
 }
 
@@ -681,7 +694,7 @@ void launch_tt_vertex_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, co
     if (T == 0) return;
     {
         Launch L("k_tt_vertex", s);
-        k_tt_vertex<true><<<blocks_for(T, 256), 256, 0, s>>>(tvs, T, vt_off, vt, nullptr, tt_off, tt);
+        launch_pdl(k_tt_vertex<true>, blocks_for(T, 256), 256, 0, s, tvs, T, vt_off, vt, nullptr, tt_off, tt);
     }
 }
 

@@ -81,6 +81,7 @@ __device__ __forceinline__ int64_t block_exclusive_scan(int64_t x, int64_t &excl
 
 __global__ void __launch_bounds__(kThreads) k_scan(ScanParams p)
 {
+    griddep_wait();
     const int jb = blockIdx.y;
     if (jb >= p.n_jobs) return;
     const ScanJob &j = p.job[jb];
@@ -150,7 +151,7 @@ void scan_batch(const ScanJob *jobs, int n_jobs, ScanWorkspace &ws, DevStatus *s
     dim3 grid((unsigned)max_tiles, n_jobs);
     {
         Launch L("k_scan", s);
-        k_scan<<<grid, kThreads, 0, s>>>(p);
+        launch_pdl(k_scan, grid, kThreads, 0, s, p);
     }
     scan_ws_end(ws, s);
 }

@@ -427,6 +427,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
 
 __global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
 {
+    griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
@@ -692,6 +693,7 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
 
 __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
 {
+    griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(StageM<unsigned long long>)];
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
     stage_rows_b(S, b);
@@ -710,6 +712,7 @@ k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank
              const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t T,
              int *__restrict__ fv, int *__restrict__ ft, int64_t *__restrict__ ff_off)
 {
+    griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= T) return;
     const int sh = (int)(c & 7) * 4;
@@ -769,6 +772,7 @@ __global__ void __launch_bounds__(kVtsThreads)
 k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt,
           const int4 *__restrict__ tvs, uint32_t *__restrict__ vflag, int64_t *__restrict__ vkey)
 {
+    griddep_wait();
     __shared__ int cell[kCap], out[kCap], meta[kCap];
     __shared__ int s_vlo, s_vhi, s_n;
     __shared__ long long s_base;
@@ -905,6 +909,7 @@ __device__ __forceinline__ uint32_t slot_bits(const EdgeOffsets &p, long long s0
 
 __global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets(EdgeOffsets p)
 {
+    griddep_wait();
     {
         const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.next_words;
@@ -993,6 +998,7 @@ __global__ void __launch_bounds__(256)
 k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int win_size,
                 int *__restrict__ win, int64_t n_win2, int win_size2, int *__restrict__ win2)
 {
+    griddep_wait();
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v > V) return;
     const long long lo = v == 0 ? -1 : off[v - 1];
@@ -1017,6 +1023,7 @@ k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__r
                const uint2 *__restrict__ vrank, int64_t nwk, int *__restrict__ vorder,
                int *__restrict__ dcount)
 {
+    griddep_wait();
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     // the positions past the vertices with cells (their rows are empty)
@@ -1047,6 +1054,7 @@ __global__ void __launch_bounds__(256, TG_VTP_MINB)
 k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int64_t V,
            const int64_t *__restrict__ vt_off, const int *__restrict__ vt, int *__restrict__ vtp)
 {
+    griddep_wait();
     const int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
     const int lane = threadIdx.x & 31;
     if (r0 >= V) return;  // warp-uniform
@@ -1086,6 +1094,7 @@ __global__ void __launch_bounds__(256)
 k_seg_ranks(const int64_t *__restrict__ seg_c, int64_t n, const uint2 *__restrict__ erank,
             const uint2 *__restrict__ frank, int64_t *__restrict__ seg_ef)
 {
+    griddep_wait();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i > n) return;
     seg_ef[i] = rank_of(erank, 6LL * seg_c[i]);
@@ -1106,7 +1115,7 @@ void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int 
                           int32_t *win, cudaStream_t s, int win_size2, int32_t *win2)
 {
     Launch L("k_window_starts", s);
-    k_window_starts<<<(unsigned)((V + 1 + 255) / 256), 256, 0, s>>>(
+    launch_pdl(k_window_starts, (unsigned)((V + 1 + 255) / 256), 256, 0, s,
         off, V, window_count(n_entries, win_size), win_size, win,
         win2 ? window_count(n_entries, win_size2) : 0, win_size2, win2);
 }
@@ -1140,7 +1149,7 @@ void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4
     scan_ws_begin(ws, s, &p.tiles, &p.next, &p.next_words);
     {
         Launch L("k_edge_offsets", s);
-        k_edge_offsets<<<(unsigned)std::max<int64_t>(tiles, 1), kEdgeThreads, 0, s>>>(p);
+        launch_pdl(k_edge_offsets, (unsigned)std::max<int64_t>(tiles, 1), kEdgeThreads, 0, s, p);
     }
     scan_ws_end(ws, s);
 }
@@ -1149,7 +1158,7 @@ void launch_star_a(const StarA &a, cudaStream_t s)
 {
     if (a.V == 0) return;
     Launch L("k_star_a", s);
-    k_star_a<<<n_windows(a.nvt), kThreads, 0, s>>>(a);
+    launch_pdl(k_star_a, n_windows(a.nvt), kThreads, 0, s, a);
 }
 
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
@@ -1158,7 +1167,7 @@ void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *b
 {
     if (T == 0) return;
     Launch L("k_face_slots", s);
-    k_face_slots<<<(unsigned)((T + 255) / 256), 256, 0, s>>>(fflag, frank, brank, tvs, T, fv, ft,
+    launch_pdl(k_face_slots, (unsigned)((T + 255) / 256), 256, 0, s, fflag, frank, brank, tvs, T, fv, ft,
                                                             ff_off);
 }
 
@@ -1166,7 +1175,7 @@ void launch_star_b(const StarB &b, cudaStream_t s)
 {
     if (b.V == 0) return;
     Launch L("k_star_b", s);
-    k_star_b<<<n_windows_b(b.nvt), kThreads, 0, s>>>(b);
+    launch_pdl(k_star_b, n_windows_b(b.nvt), kThreads, 0, s, b);
 }
 
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
@@ -1174,7 +1183,7 @@ void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int6
 {
     if (V == 0) return;
     Launch L("k_vt_sort", s);
-    k_vt_sort<<<n_windows(nvt), kVtsThreads, 0, s>>>(vt_off, win, vt, tvs, vflag, vkey);
+    launch_pdl(k_vt_sort, n_windows(nvt), kVtsThreads, 0, s, vt_off, win, vt, tvs, vflag, vkey);
 }
 
 
@@ -1184,7 +1193,7 @@ void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
 {
     if (V == 0) return;
     Launch L("k_vorder_place", s);
-    k_vorder_place<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vt_off, V, vkey, vrank, nwk,
+    launch_pdl(k_vorder_place, (unsigned)((V + 255) / 256), 256, 0, s, vt_off, V, vkey, vrank, nwk,
                                                                 vorder, dcount);
 }
 
@@ -1193,7 +1202,7 @@ void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, cons
 {
     if (V == 0) return;
     Launch L("k_vtp_fill", s);
-    k_vtp_fill<<<(unsigned)((V + 255) / 256), 256, 0, s>>>(vorder, pofs, V, vt_off, vt, vtp);
+    launch_pdl(k_vtp_fill, (unsigned)((V + 255) / 256), 256, 0, s, vorder, pofs, V, vt_off, vt, vtp);
 }
 
 
@@ -1201,7 +1210,7 @@ void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const
                       int64_t *seg_ef, cudaStream_t s)
 {
     Launch L("k_seg_ranks", s);
-    k_seg_ranks<<<(unsigned)((n + 1 + 255) / 256), 256, 0, s>>>(seg_c, n, erank, frank, seg_ef);
+    launch_pdl(k_seg_ranks, (unsigned)((n + 1 + 255) / 256), 256, 0, s, seg_c, n, erank, frank, seg_ef);
 }
 
 }  // namespace tg
