@@ -703,46 +703,38 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
         star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b);
 }
 
-// The faces in id order, one thread per cell: the cell's first-occurrence
-// bits (4 per cell, 8 cells per flag word) with the rank of the first give
-// the ids of the faces first seen in it; writes FV, FT's first cell and the
-// FF offsets (3 * (2 * id - boundary faces before it)).
+// The faces in id order, one thread per face occurrence q = 4 cell + col (a
+// warp covers eight cells): a first occurrence (its bit in fflag) gets its id
+// from the rank words and writes FV, FT's first cell and the FF offset
+// (3 * (2 * id - boundary faces before it)); consecutive lanes holding faces
+// write consecutive ids.
 __global__ void __launch_bounds__(256)
 k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank,
              const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t T,
              int *__restrict__ fv, int *__restrict__ ft, int64_t *__restrict__ ff_off)
 {
     griddep_wait();
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= T) return;
-    const int sh = (int)(c & 7) * 4;
-    const uint32_t word = __ldg(fflag + (c >> 3));
-    const uint32_t bits = (word >> sh) & 0xfu;
-    if (!bits) return;
-    const uint2 fr = __ldg(frank + (c >> 3));
-    int fid = (int)fr.y + __popc(word & ((1u << sh) - 1u));
-    const int4 w = __ldg(tvs + c);
-    uint2 br = make_uint2(0, 0);
-    if (ff_off) br = __ldg(brank + (c >> 3));
-#pragma unroll
-    for (int col = 0; col < 4; col++) {
-        if (!((bits >> col) & 1u)) continue;
-        if (fv) {
-            // the face omits slot 3 - col
-            const int o0 = col == 3 ? w.y : w.x;
-            const int o1 = col >= 2 ? w.z : w.y;
-            const int o2 = col >= 1 ? w.w : w.z;
-            fv[3LL * fid] = o0;
-            fv[3LL * fid + 1] = o1;
-            fv[3LL * fid + 2] = o2;
-        }
-        if (ft) ft[2LL * fid] = (int)c;
-        if (ff_off) {
-            const int qb = sh + col;
-            const int nb = (int)br.y + __popc(br.x & ((1u << qb) - 1u));
-            ff_off[fid] = 3LL * (2LL * fid - nb);
-        }
-        fid++;
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 4 * T) return;
+    const uint32_t word = __ldg(fflag + (q >> 5));
+    const int b = (int)(q & 31);
+    if (!((word >> b) & 1u)) return;
+    const uint2 fr = __ldg(frank + (q >> 5));
+    const int fid = (int)fr.y + __popc(word & ((1u << b) - 1u));
+    const int64_t c = q >> 2;
+    const int col = (int)(q & 3);
+    if (fv) {
+        // the face omits slot 3 - col
+        const int4 w = __ldg(tvs + c);
+        fv[3LL * fid] = col == 3 ? w.y : w.x;
+        fv[3LL * fid + 1] = col >= 2 ? w.z : w.y;
+        fv[3LL * fid + 2] = col >= 1 ? w.w : w.z;
+    }
+    if (ft) ft[2LL * fid] = (int)c;
+    if (ff_off) {
+        const uint2 br = __ldg(brank + (q >> 5));
+        const int nb = (int)br.y + __popc(br.x & ((1u << b) - 1u));
+        ff_off[fid] = 3LL * (2LL * fid - nb);
     }
 }
 
@@ -1167,8 +1159,8 @@ void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *b
 {
     if (T == 0) return;
     Launch L("k_face_slots", s);
-    launch_pdl(k_face_slots, (unsigned)((T + 255) / 256), 256, 0, s, fflag, frank, brank, tvs, T, fv, ft,
-                                                            ff_off);
+    launch_pdl(k_face_slots, (unsigned)((4 * T + 255) / 256), 256, 0, s, fflag, frank, brank,
+               tvs, T, fv, ft, ff_off);
 }
 
 void launch_star_b(const StarB &b, cudaStream_t s)
