@@ -115,8 +115,7 @@ struct StageBaseA {
     int vid[kCap];
     int meta[kCap];                     // row start | D << 10 | slot of v << 20
     unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
-    short cslot[kCap][4];               // hash slot of each entry's 3 candidates (other vertices)
-    int cnt[kCap];                      // per row start: neighbours counted / listed so far
+    short cslot[kCap][3];               // hash slot of each entry's 3 candidates (other vertices)
     int n, vlo, vhi, full, wide;
     long long base;
 };
@@ -226,7 +225,6 @@ __device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
             S.vid[rs + j] = v;
             S.meta[rs + j] = rs | (D << 10);
         }
-        S.cnt[rs] = 0;
     }
     __syncthreads();
     return !S.full;
@@ -325,12 +323,16 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 template <typename M>
 __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_work)
 {
-    // first sightings of owned edges (entry << 2 | candidate), in the hash
-    // keys' space: after the table is built only its masks are read
-    static_assert(sizeof(S.hkey) >= 3 * kCap * sizeof(int), "work list does not fit the keys");
+    // in the hash keys' space once the table is built (only its masks are
+    // read after that): the first sightings of owned edges (entry << 2 |
+    // candidate), then per row start the count of neighbours
+    static_assert(sizeof(S.hkey) >= 4 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
+    int *cnt = work + 3 * kCap;
     if (!stage_cells_and_hash(S, a.vtp, a.tvs, a.vorder, a.st)) return;
     const int n = S.n;
+    for (int e = threadIdx.x; e < n; e += blockDim.x)
+        if (m_rs(S.meta[e]) == e) cnt[e] = 0;
     if (threadIdx.x == 0) n_work = 0;
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -347,7 +349,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (mctz(cm[k]) != pos) continue;                  // not the first sighting
-            atomicAdd(&S.cnt[rs], 1);
+            atomicAdd(&cnt[rs], 1);
             if (get4(w, k + (k >= sv)) > v) work[atomicAdd(&n_work, 1)] = (e << 2) | k;
         }
         if (sv <= 1) {
@@ -416,7 +418,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
         if (m_rs(m) != e) continue;
-        const int d = S.cnt[e];
+        const int d = cnt[e];
         a.deg[S.vid[e]] = d;
         if (d > kMaxDeg) {
             atomicOr(&a.st->flags, ST_HEAVY_DEG);
@@ -425,7 +427,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 7) k_star_a(StarA a)
+__global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 {
     griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
