@@ -901,7 +901,12 @@ __device__ __forceinline__ uint32_t slot_bits(const EdgeOffsets &p, long long s0
     return kEdgeItems == 32 ? w : (w >> (s0 & 31)) & ((1u << kEdgeItems) - 1u);
 }
 
-__global__ void __launch_bounds__(kEdgeThreads) k_edge_offsets(EdgeOffsets p)
+// eight blocks per SM (32 registers): the extra resident blocks hide the
+// gathers' latency better than the few spilled registers cost
+#ifndef TG_EDGE_MINB
+#define TG_EDGE_MINB 8
+#endif
+__global__ void __launch_bounds__(kEdgeThreads, TG_EDGE_MINB) k_edge_offsets(EdgeOffsets p)
 {
     griddep_wait();
     {
