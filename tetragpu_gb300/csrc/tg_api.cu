@@ -449,15 +449,9 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         int32_t *vv, *eid_sorted = nullptr;
         int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
         int64_t *ff_off = nullptr;
-        TRY(dalloc(&vv, nvv, s));
-        tmp.track(vv);
-        if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
+        // each kernel goes out once its own buffers exist; the later
+        // allocations are made while it runs
         if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
-        if (need_te) TRY(tmp.alloc(&te, 6 * T));
-        if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
-        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
-        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
-        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
         // id-ordered passes over the occurrence slots
         if (et_off || ef_off || ee_off || ev) {
             uint32_t *len;
@@ -465,7 +459,15 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
                                 ev, len, m->scan, m->st, s);
         }
+        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
+        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
+        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
         if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, s);
+        TRY(dalloc(&vv, nvv, s));
+        tmp.track(vv);
+        if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
+        if (need_te) TRY(tmp.alloc(&te, 6 * T));
+        if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
         // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
         // only when EE is wanted); TT and FF from the boundary-face count
         int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
