@@ -15,8 +15,9 @@
 // most kWin + kMaxStar - 1 entries), stages their cells and the cells' sorted
 // TV rows in shared memory (all gathers in flight at once), and gives one
 // thread to each (vertex, star cell) entry.  In pass A a shared-memory hash
-// keyed by (vertex, neighbour) holds, per neighbour, the 64-bit mask of star
-// positions whose cell contains it; lanes holding the same key are merged by
+// keyed by (vertex, neighbour) holds, per neighbour, the mask of star
+// positions whose cell contains it (32-bit in a window whose stars have at
+// most 32 cells, else 64-bit); lanes holding the same key are merged by
 // __match_any_sync first, so one lane per group touches the table.  Pass A
 // leaves every entry's three candidate masks in global memory and pass B
 // stages them instead of rebuilding the table.  With the masks, "first
@@ -29,9 +30,9 @@
 //             neighbour counts, the candidate masks
 //   k_star_b  ids (ranks of first occurrences), sorted VV rows, id-sorted
 //             incident edge ids, TE, TF, FT's second cell, ET and EF rows
-//   k_edge_offsets_* / k_face_slots  the id-ordered passes over occurrence
-//             slots: ET / EF / EE offsets and EV; FV, FT's first cell, FF
-//             offsets
+//   k_edge_offsets / k_face_slots  the id-ordered passes over occurrence
+//             slots: ET / EF / EE offsets and EV (one pass with a look-back
+//             scan); FV, FT's first cell, FF offsets
 #include "tg_internal.h"
 
 namespace tg {
