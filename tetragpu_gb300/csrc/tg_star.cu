@@ -107,6 +107,7 @@ __device__ __forceinline__ int mctz(unsigned long long m) { return __ffsll((long
 __device__ __forceinline__ int mpopc(unsigned m) { return __popc(m); }
 __device__ __forceinline__ int mpopc(unsigned long long m) { return __popcll(m); }
 constexpr int kNarrowStar = 32;   // the most cells a star may have for 32-bit masks
+constexpr int kRowBoundary = 1 << 30;   // pass A's per-row count word: v has a boundary face
 
 // Pass A's shared memory: the fields that do not depend on the mask width
 // first (staged before the width is chosen), the masks last.
@@ -353,6 +354,11 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
             atomicAdd(&cnt[rs], 1);
             if (get4(w, k + (k >= sv)) > v) work[atomicAdd(&n_work, 1)] = (e << 2) | k;
         }
+        // a face at v held by this cell alone (the AND of its two other
+        // vertices' masks is this position's bit): v is on the boundary
+        const M bit = (M)1 << pos;
+        if ((cm[0] & cm[1]) == bit || (cm[0] & cm[2]) == bit || (cm[1] & cm[2]) == bit)
+            atomicOr(&cnt[rs], kRowBoundary);
         if (sv <= 1) {
             // faces whose lowest vertex is v: omit slot 1, 2, 3 when v is in
             // slot 0; omit slot 0 when v is in slot 1.  The face's other two
@@ -374,10 +380,13 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
         }
     }
     __syncthreads();
-    // the edges v owns, kEfLanesA lanes to an edge (each lane every
-    // kEfLanesA-th cell of the edge's star): flag the first occurrence and
-    // record the ET and EF row lengths at that occurrence slot.  A face
-    // (v,u,x) is counted in the first cell holding u and x.
+    // the edges v owns, kEfLanesA lanes to an edge: flag the first
+    // occurrence and record the ET and EF row lengths at that occurrence
+    // slot.  At a vertex with no boundary face every face (v,u,x) lies in
+    // two cells of the edge's star and every cell holds two of them, so an
+    // edge has as many faces as cells; at a boundary vertex each lane takes
+    // every kEfLanesA-th cell of the edge's star and counts the faces (v,u,x)
+    // whose first cell it is.
     const int nw = n_work;
     constexpr int L = kEfLanesA;
     const int span = ((nw * L + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
@@ -394,7 +403,8 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
             const int u = get4(S.tv[e], t);
             mu = S.hmask[S.cslot[e][k]];
             p = 6 * S.cell[e] + pair_slot(sv, t);
-            M mm = mu;
+            M mm = (cnt[rs] & kRowBoundary) ? mu : 0;
+            if (!mm && sub == 0) n_ef = mpopc(mu);
             for (int q = 0; q < sub; q++) mm &= mm - 1;
             while (mm) {
                 const int j = mctz(mm);
@@ -419,7 +429,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
         if (m_rs(m) != e) continue;
-        const int d = cnt[e];
+        const int d = cnt[e] & ~kRowBoundary;
         a.deg[S.vid[e]] = d;
         if (d > kMaxDeg) {
             atomicOr(&a.st->flags, ST_HEAVY_DEG);
