@@ -43,15 +43,16 @@ constexpr int kAdjThreads = TG_ADJ_THREADS;
 // u's row (urow, un entries; read four at a time from 16-byte boundaries
 // when the array is aligned: i from i0 = -(ub mod 4), one load instruction
 // per four entries; else one entry at a time) against v's row (row, d
-// entries, shared memory): each w found at position lo of v's row sets bit lo
-// of bits_v and bit i of bits_u; pv = v's place in u's row.  The search is
-// branch-free with a fixed number of steps (TOP, TOP/2, .. 1; TOP the highest
-// power of 2 the row length can need; the first step only for rows longer
-// than TOP), so the lanes of a warp stay together.
+// entries, shared memory, padded with INT_MAX to top = the power of two at or
+// above d): each w found at position lo of v's row sets bit lo of bits_v and
+// bit i of bits_u; pv = v's place in u's row.  The search takes the steps
+// top / 2, .. 1 (those above top / 2 skipped by a per-thread predicate, so
+// the lanes of a warp stay together) and needs no bound: every probe lies in
+// the padded row.
 template <typename M, int TOP>
-__device__ __forceinline__ void adj_scan(const int *row, int d, const int *__restrict__ urow,
-                                         int i0, int un, int lim, bool vec, int v, M &bits_v,
-                                         M &bits_u, int &pv)
+__device__ __forceinline__ void adj_scan(const int *row, int d, int top,
+                                         const int *__restrict__ urow, int i0, int un, int lim,
+                                         bool vec, int v, M &bits_v, M &bits_u, int &pv)
 {
     // the next four entries are loaded while the current four are searched
     auto load4 = [&](int j) -> int4 {
@@ -68,25 +69,25 @@ __device__ __forceinline__ void adj_scan(const int *row, int d, const int *__res
         const int4 cur = nxt;
         if (i0 + 4 < un) nxt = load4(i0 + 4);
         const int q[4] = {cur.x, cur.y, cur.z, cur.w};
+        // four searches in lock step (independent shared-memory loads in
+        // flight together); entries outside [0, un) search harmlessly and
+        // set nothing
+        int lo[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int step = TOP / 2; step > 0; step >>= 1) {
+            if (2 * step > top) continue;
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                lo[t] += row[lo[t] + step - 1] < q[t] ? step : 0;
+        }
 #pragma unroll
         for (int t = 0; t < 4; t++) {
             const int i = i0 + t;
-            if (i < 0 || i >= un) continue;
-            const int w = q[t];
-            if (w == v) {
-                pv = i;
-                continue;
-            }
-            // entries of v's row below w; the largest step only for a row
-            // that can need it (rows of up to TOP entries take one step less)
-            int lo = d > TOP && row[TOP - 1] < w ? TOP : 0;
-#pragma unroll
-            for (int step = TOP / 2; step > 0; step >>= 1)
-                if (lo + step <= d && row[lo + step - 1] < w) lo += step;
-            if (lo < d && row[lo] == w) {
-                bits_v |= (M)1 << lo;
-                bits_u |= (M)1 << i;
-            }
+            const bool valid = i >= 0 && i < un;
+            if (valid && q[t] == v) pv = i;
+            const bool hit = valid && q[t] != v && row[lo[t]] == q[t];
+            bits_v |= (M)hit << lo[t];
+            bits_u |= (M)hit << (i & (8 * (int)sizeof(M) - 1));
         }
     }
 }
@@ -97,6 +98,7 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
 {
     griddep_wait();
     __shared__ int nb[kAdjCap];
+    __shared__ int prow[2 * kAdjCap];   // the row starting at rs at 2 rs, INT_MAX to 2 rs + 2 d
     __shared__ int meta[kAdjCap];   // row start | row length << 16
     __shared__ int vid[kAdjCap];
     __shared__ int own[kAdjCap];
@@ -133,8 +135,12 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) nb[e] = __ldg(vv + base + e);
     __syncthreads();
-    for (int e = threadIdx.x; e < n; e += blockDim.x)
-        if ((meta[e] >> 16) <= kMaxDeg && nb[e] > vid[e]) own[atomicAdd(&n_own, 1)] = e;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int m = meta[e], rs = m & 0xffff, d = m >> 16;
+        prow[rs + e] = nb[e];            // 2 rs + (e - rs)
+        prow[rs + e + d] = INT_MAX;
+        if (d <= kMaxDeg && nb[e] > vid[e]) own[atomicAdd(&n_own, 1)] = e;
+    }
     __syncthreads();
     const int no = n_own;
     const bool vec = (reinterpret_cast<uintptr_t>(vv) & 15) == 0;
@@ -149,16 +155,18 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
         const int lim = (int)min(n_vv - ub, (int64_t)INT_MAX);
         int pv = -1;
         unsigned long long bv, bu;
+        const int top = d <= 1 ? 1 : 1 << (32 - __clz(d - 1));
         if (d <= 32 && un <= 32) {   // both masks fit 32 bits (the common case)
             unsigned bv32 = 0u, bu32 = 0u;
-            adj_scan<unsigned, 16>(nb + rs, d, vv + ub, vec ? -(int)(ub & 3) : 0, un, lim, vec, v,
-                                   bv32, bu32, pv);
+            adj_scan<unsigned, 32>(prow + 2 * rs, d, top, vv + ub, vec ? -(int)(ub & 3) : 0, un,
+                                   lim, vec, v, bv32, bu32, pv);
             bv = bv32;
             bu = bu32;
         } else {
             bv = bu = 0ull;
-            adj_scan<unsigned long long, 32>(nb + rs, d, vv + ub, vec ? -(int)(ub & 3) : 0, un,
-                                             lim, vec, v, bv, bu, pv);
+            adj_scan<unsigned long long, 64>(prow + 2 * rs, d, top, vv + ub,
+                                             vec ? -(int)(ub & 3) : 0, un, lim, vec, v, bv, bu,
+                                             pv);
         }
         adj[base + e] = bv;
         if (pv >= 0) adj[ub + pv] = bu;
