@@ -157,6 +157,95 @@ struct PinnedPool {
 };
 PinnedPool g_pinned;
 
+// Side streams for kernels of one extraction that need nothing from each
+// other (the face slots beside the edge offsets; FE / TT and FF beside EE):
+// a stream and its fork / join events, kept per device and reused, so that a
+// mesh built per request creates none.
+struct SideLane {
+    int device = 0;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+struct SidePool {
+    std::mutex mu;
+    std::vector<SideLane *> free_lanes;
+    SideLane *get(int device)
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (size_t i = 0; i < free_lanes.size(); i++)
+                if (free_lanes[i]->device == device) {
+                    SideLane *l = free_lanes[i];
+                    free_lanes.erase(free_lanes.begin() + (std::ptrdiff_t)i);
+                    return l;
+                }
+        }
+        SideLane *l = new SideLane();
+        l->device = device;
+        if (cudaStreamCreateWithFlags(&l->s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&l->fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&l->join, cudaEventDisableTiming) != cudaSuccess) {
+            (void)cudaGetLastError();
+            if (l->s) cudaStreamDestroy(l->s);
+            if (l->fork) cudaEventDestroy(l->fork);
+            delete l;
+            return nullptr;
+        }
+        return l;
+    }
+    void put(SideLane *l)
+    {
+        if (!l) return;
+        std::lock_guard<std::mutex> lk(mu);
+        free_lanes.push_back(l);
+    }
+};
+SidePool g_side;
+
+// One fork of an extraction's stream: the stream fork() returns runs what it
+// is given after everything enqueued on the main stream before the call;
+// join() makes the main stream wait for that work.  The destructor joins, so
+// declared after the extraction's temporaries it orders their frees after
+// the side work, on every return path.  Without a side stream (none could
+// be made) fork() returns the main stream itself.
+struct Fork {
+    cudaStream_t main;
+    int device;
+    SideLane *lane = nullptr;
+    bool open = false;
+    Fork(cudaStream_t s, int dev) : main(s), device(dev) {}
+    cudaStream_t fork()
+    {
+        join();
+        if (!lane) lane = g_side.get(device);
+        if (!lane) return main;
+        if (cudaEventRecord(lane->fork, main) != cudaSuccess ||
+            cudaStreamWaitEvent(lane->s, lane->fork, 0) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return main;
+        }
+        open = true;
+        return lane->s;
+    }
+    void join()
+    {
+        if (!open) return;
+        open = false;
+        if (cudaEventRecord(lane->join, lane->s) != cudaSuccess ||
+            cudaStreamWaitEvent(main, lane->join, 0) != cudaSuccess) {
+            // the main stream cannot be ordered after the side stream: wait
+            // for it from the host instead
+            (void)cudaGetLastError();
+            cudaStreamSynchronize(lane->s);
+        }
+    }
+    ~Fork()
+    {
+        join();
+        g_side.put(lane);
+    }
+};
+
 struct Rel {
     int64_t rows = 0, entries = 0;
     int width = 0;
@@ -368,6 +457,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
     const int64_t *vt_off = m->rel[TG_REL_VT].off;
     const int32_t *vt = m->rel[TG_REL_VT].ent;
     Temps tmp(s);
+    Fork side(s, m->device);   // after tmp: joined before its frees
 
     if (want_star) {
         // the status is clean: the read-back that ended the last call reset it
@@ -452,17 +542,20 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         // each kernel goes out once its own buffers exist; the later
         // allocations are made while it runs
         if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
-        // id-ordered passes over the occurrence slots
+        // the id-ordered passes over the occurrence slots: the face slots on
+        // a side stream beside the edge offsets (a look-back scan that leaves
+        // issue slots free), joined before pass B
+        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
+        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
+        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
+        if (fv || ft || ff_off)
+            launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, side.fork());
         if (et_off || ef_off || ee_off || ev) {
             uint32_t *len;
             TRY(tmp.alloc(&len, E));
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
                                 ev, len, m->scan, m->st, s);
         }
-        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
-        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
-        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
-        if (fv || ft || ff_off) launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, s);
         TRY(dalloc(&vv, nvv, s));
         tmp.track(vv);
         if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
@@ -494,6 +587,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
+        side.join();
         launch_star_b(b, s);
         tmp.keep(vv);
         tmp.keep(vv_off);
@@ -503,15 +597,18 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             m->cadj = nullptr;
         }
 
-        if (fe || tt || ff_off)
-            launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s);
-        if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s);
-        // an edge (a,b) has deg(a) + deg(b) - 2 EE entries: sum deg^2 - 2E in all
-        const int64_t n_ee = sum_deg_sq - 2 * E;
-        if (ee_off) {
-            TRY(dalloc(&ee, n_ee, s));
-            launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+        // the cell-ordered FE / TT and FF rows on a side stream beside EE
+        // (each reads only what pass B and the passes before it wrote)
+        const int64_t n_ee = sum_deg_sq - 2 * E;   // deg(a) + deg(b) - 2 per edge (a,b)
+        if (ee_off) TRY(dalloc(&ee, n_ee, s));
+        if (fe || tt || ff_off || ff) {
+            const cudaStream_t s2 = side.fork();
+            if (fe || tt || ff_off)
+                launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s2);
+            if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
         }
+        if (ee_off) launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+        side.join();
         CK(cudaGetLastError());
 
         auto give_fixed = [&](int r, int32_t *p, int64_t rows) {
