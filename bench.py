@@ -294,14 +294,14 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
 
     def batch_step():
         with tg.Batch(d_tv.data_ptr(), nv, n_cells=nc, on_device=True, stream=s) as b:
-            b.extract(tg.ALL_RELATIONS, stream=s)
+            b.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
             b.critical_points(d_f.data_ptr(), on_device=True, out_ptr=d_cls.data_ptr(), stream=s)
 
     def loop_step():
         for i in range(len(meshes)):
             with tg.Mesh(d_tv.data_ptr() + 16 * int(c_off[i]), int(nv[i]), n_cells=int(nc[i]),
                          on_device=True, stream=s) as g:
-                g.extract(tg.ALL_RELATIONS, stream=s)
+                g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
                 g.critical_points(d_f.data_ptr() + 4 * int(v_off[i]), on_device=True,
                                   out_ptr=d_cls.data_ptr() + 12 * int(v_off[i]), stream=s)
 
@@ -365,7 +365,7 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
             for k in range(n_steps):
                 es = e_streams[k % 2].cuda_stream
                 b = tg.Batch(d_tv2[k % 2].data_ptr(), nv, n_cells=nc, on_device=True, stream=es)
-                b.extract(tg.ALL_RELATIONS, stream=es)
+                b.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=es)
                 tg._lib.check(lib.tg_batch_critical_points(b._h, d_f2[k % 2].data_ptr(),
                                                            tg.FIELD_F32, 1,
                                                            d_cls2[k % 2].data_ptr(), 1, es))
@@ -502,7 +502,7 @@ def main_serve(args, torch, tg, rank):
         if q[0] == "mesh":
             m = pool[q[1]]
             g = tg.Mesh(m.tv, m.n_verts, stream=s)
-            g.extract(tg.ALL_RELATIONS, stream=s)
+            g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
             g.critical_points(m.fields[q[2]], stream=s)
             b = g.device_bytes()
             while order and used + b > budget:
@@ -517,7 +517,7 @@ def main_serve(args, torch, tg, rank):
             m = pool[reqs[q[1]][1]]
             if resident.get(q[1]) is None:  # evicted: rebuild
                 g = tg.Mesh(m.tv, m.n_verts, stream=s)
-                g.extract(tg.ALL_RELATIONS, stream=s)
+                g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
                 resident[q[1]] = (g, g.device_bytes())
                 order.append(q[1])
                 used += resident[q[1]][1]
@@ -604,7 +604,7 @@ def main():
 
     def step():
         with tg.Mesh(d_tv.data_ptr(), V, n_cells=T, on_device=True, stream=s) as g:
-            g.extract(tg.ALL_RELATIONS, stream=s)
+            g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
             g.critical_points(d_field.data_ptr(), on_device=True, out_ptr=d_classes.data_ptr(),
                               stream=s)
             info = {"counts": g.counts()}
@@ -706,7 +706,7 @@ def main():
             es = e_streams[k % 2].cuda_stream
             h_ent, h_off, h_cls = bufs[k % 2]
             g = tg.Mesh(d_tv2[k % 2].data_ptr(), V, n_cells=T, on_device=True, stream=es)
-            g.extract(tg.ALL_RELATIONS, stream=es)
+            g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=es)
             tg._lib.check(lib.tg_critical_points(g._h, d_f2[k % 2].data_ptr(), tg.FIELD_F32, 1,
                                                  d_cls2[k % 2].data_ptr(), 1, es))
             if k + 1 < n_steps:

@@ -84,6 +84,10 @@ enum {
 
 /* tg_extract options */
 #define TG_OPT_TT_VERTEX_SHARING 0x1u /* TT = cells sharing >= 1 vertex (default: sharing a face) */
+/* Also build the field-independent half of tg_critical_points (the link
+ * adjacency over VV, kept on the mesh) during the extraction, beside its last
+ * kernels, for a caller that classifies fields next.  Needs VV in the mask. */
+#define TG_OPT_LINK_ADJACENCY 0x2u
 
 /* critical-point field types */
 #define TG_FIELD_F32 0

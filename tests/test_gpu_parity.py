@@ -107,6 +107,29 @@ def test_critical_points_ties_broken_by_id(gpu_lib, oracle):
     assert np.array_equal(got, oracle.critical_points(tvs, m.n_verts, field.astype(np.float32)))
 
 
+@pytest.mark.parametrize("mesh", ["coned", "wide"])
+def test_link_adjacency_prepared_during_extraction(gpu_lib, oracle, mesh):
+    # the field-independent half of critical points built beside the last
+    # extraction kernels (a side stream) gives the same relations and classes
+    if mesh == "coned":
+        m = meshgen.kuhn_mesh(10, 0.3, seed=11)
+        tv, nv = m.tv, m.n_verts
+        field = meshgen.gaussian_mixture_field(m.coords, n_gauss=6, seed=12).astype(np.float32)
+    else:   # stars and VV rows beyond 32: the 64-bit masks
+        rng = np.random.default_rng(13)
+        tv, nv = _ring(40, rng=rng)
+        field = rng.standard_normal(nv).astype(np.float32)
+    tvs = oracle.canonicalize(tv, nv)
+    ref = oracle.extract(tvs, nv)
+    with gpu_lib.Mesh(tv, nv) as g:
+        g.extract(gpu_lib.ALL_RELATIONS, options=gpu_lib.OPT_LINK_ADJACENCY)
+        assert_relations_equal({n: g.relation(n) for n in RELS}, ref)
+        got = g.critical_points(field)
+        got2 = g.critical_points(-field)   # the prepared adjacency serves a second field
+    assert np.array_equal(got, oracle.critical_points(tvs, nv, field))
+    assert np.array_equal(got2, oracle.critical_points(tvs, nv, -field))
+
+
 def test_irregular_full(gpu_lib, oracle):
     """The 64^3, 20%-coned workload: all 13 relations and critical points."""
     m = meshgen.workload_irregular()

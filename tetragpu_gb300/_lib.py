@@ -18,6 +18,7 @@ RELATIONS = ["validate", "TE", "EV", "ET", "TF", "FV", "FE", "FT", "EF", "VT",
 REL = {name: i for i, name in enumerate(RELATIONS)}
 ALL_RELATIONS = 0x3FFE
 OPT_TT_VERTEX_SHARING = 0x1
+OPT_LINK_ADJACENCY = 0x2
 FIELD_F32, FIELD_F64 = 0, 1
 
 STATUS = {0: "TG_OK", 1: "TG_ERR_INVALID_ARGUMENT", 2: "TG_ERR_INVALID_MESH", 3: "TG_ERR_CUDA",

@@ -597,15 +597,26 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             m->cadj = nullptr;
         }
 
-        // the cell-ordered FE / TT and FF rows on a side stream beside EE
-        // (each reads only what pass B and the passes before it wrote)
+        // the cell-ordered FE / TT and FF rows, and on request the link
+        // adjacency of critical points, on a side stream beside EE (each
+        // reads only what pass B and the passes before it wrote)
         const int64_t n_ee = sum_deg_sq - 2 * E;   // deg(a) + deg(b) - 2 per edge (a,b)
         if (ee_off) TRY(dalloc(&ee, n_ee, s));
-        if (fe || tt || ff_off || ff) {
+        const bool prep_adj = (opts & TG_OPT_LINK_ADJACENCY) && (mask & TG_VV);
+        int32_t *vv_win = nullptr;
+        if (prep_adj) {
+            TRY(dalloc(&m->cadj, nvv, s));
+            TRY(tmp.alloc(&vv_win, window_count(nvv, crit_window()) + 1));
+        }
+        if (fe || tt || ff_off || ff || prep_adj) {
             const cudaStream_t s2 = side.fork();
             if (fe || tt || ff_off)
                 launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s2);
             if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
+            if (prep_adj) {
+                launch_window_starts(vv_off, V, nvv, crit_window(), vv_win, s2);
+                launch_crit_adj(vv_off, vv, vv_win, V, nvv, m->cadj, m->st, s2);
+            }
         }
         if (ee_off) launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
         side.join();

@@ -256,7 +256,7 @@ tg_status build_batch(tg_server *S, const std::vector<std::shared_ptr<MeshRec>> 
     }
     tg_batch *b = nullptr;
     tg_status st = tg_batch_create(tv, nc.data(), nv.data(), (int64_t)n, 0, s, &b);
-    if (st == TG_OK) st = tg_batch_extract(b, S->cfg.relation_mask | TG_VV, 0, s);
+    if (st == TG_OK) st = tg_batch_extract(b, S->cfg.relation_mask | TG_VV, TG_OPT_LINK_ADJACENCY, s);
     classes.assign((size_t)V * 3, 0);
     if (st == TG_OK)
         st = tg_batch_critical_points(b, fcat.data(), ftype, 0, classes.data(), 0, s);
@@ -401,7 +401,7 @@ tg_status acquire(tg_server *S, int64_t mesh_id, cudaStream_t s, std::shared_ptr
     const int64_t nc = m->T, nv = m->V;
     tg_batch *b = nullptr;
     tg_status st = tg_batch_create(m->tv.data(), &nc, &nv, 1, 0, s, &b);
-    if (st == TG_OK) st = tg_batch_extract(b, S->cfg.relation_mask | TG_VV, 0, s);
+    if (st == TG_OK) st = tg_batch_extract(b, S->cfg.relation_mask | TG_VV, TG_OPT_LINK_ADJACENCY, s);
     std::lock_guard<std::mutex> lk(S->mu);
     S->used -= estimate(m->T, m->V);
     if (st != TG_OK) {
