@@ -59,6 +59,10 @@ def test_empty_mesh(gpu_lib):
         assert np.array_equal(off, np.zeros(8, np.int64)) and ent.size == 0
         cp = g.critical_points(np.arange(7, dtype=np.float32))
         assert (cp[:, 2] == 4).all()
+    with gpu_lib.Mesh(np.zeros((0, 4), np.int32), 7) as g:
+        g.extract(gpu_lib.ALL_RELATIONS, options=gpu_lib.OPT_LINK_ADJACENCY)
+        cp = g.critical_points(np.arange(7, dtype=np.float32))
+        assert (cp[:, 2] == 4).all()
 
 
 @pytest.mark.parametrize("bad,code", [([[0, 1, 2, 9]], 2), ([[0, 1, 1, 2]], 2), ([[0, -1, 2, 3]], 2)])
