@@ -58,6 +58,24 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_binding_constants_match_the_header():
+    # relation bits, options and field types as the header defines them
+    from tetragpu_gb300 import _lib
+    with open(os.path.join(ROOT, "include", "tetragpu.h")) as f:
+        src = f.read()
+    defs = {}
+    for name, val in re.findall(r"^#define (TG_[A-Z0-9_]+) (.+?)\s*(?:/\*.*)?$", src, re.M):
+        m = re.fullmatch(r"\(1u? << (\d+)\)", val)
+        defs[name] = 1 << int(m.group(1)) if m else int(val.rstrip("u"), 0)
+    for i, name in enumerate(_lib.RELATIONS[1:], start=1):
+        assert defs[f"TG_{name}"] == 1 << i, name
+        assert _lib.REL[name] == i
+    assert defs["TG_ALL_RELATIONS"] == _lib.ALL_RELATIONS
+    assert defs["TG_OPT_TT_VERTEX_SHARING"] == _lib.OPT_TT_VERTEX_SHARING
+    assert defs["TG_OPT_LINK_ADJACENCY"] == _lib.OPT_LINK_ADJACENCY
+    assert (defs["TG_FIELD_F32"], defs["TG_FIELD_F64"]) == (_lib.FIELD_F32, _lib.FIELD_F64)
+
+
 def test_library_loads_and_reports_without_gpu():
     import tetragpu_gb300 as tg
     assert "sm_103a" in tg.version()
