@@ -4,20 +4,31 @@ critical-point classification, in Mtets/s.
 
 A step = one pass of the path over one mesh: tg_mesh_create (row sort,
 validation, VT) + tg_extract(all 13 relations) + tg_critical_points, then the
-mesh is destroyed.  The workload is the irregular single mesh: a 64^3 Kuhn
-grid with a seeded 20% of cubes centre-coned (1,887,438 tets, 327,054
-vertices), vertex ids permuted, float32 field = 32 Gaussians + N(0, 1e-3).
+mesh is destroyed.  The default workload is the large mesh: a 128^3 Kuhn grid
+(12,582,912 tets, 2,146,689 vertices), vertex ids permuted, float32 field
+sin(ax) sin(by) sin(cz) + N(0, 1e-4).
 
-  value  device-resident inputs (TV and field already in HBM), device outputs;
-         CUDA events on the launching stream around each step; L2 flushed
-         (a 512 MB write) before every step, outside the timed window.
-  e2e    the same steps through the C ABI with HOST buffers: pinned TV and
-         field copied in, and every relation plus the classes copied back to
-         pinned host memory (tg_copy_relations_async_i32: CSR offsets as
-         int32, narrowed on the device by one launch), all inside the timed
-         window.  Steps alternate between two streams and two sets of host
-         buffers, so a step's copies back overlap the next step's extraction
-         (the host link, not the kernels, bounds this number).
+  value     device-resident inputs (TV and field already in HBM), device
+            outputs; CUDA events on the launching stream around each step; L2
+            flushed (a 512 MB write) before every step, outside the timed
+            window.
+  roofline  the whole path against HBM bandwidth: compulsory bytes of a step
+            (TV and field read once, every output written once) / step time /
+            the measured copy peak; `kernel` inside it is the dominant kernel
+            (k_star_b) on the compulsory bytes it is responsible for, timed
+            live with CUDA events on its stream.
+  e2e       the same steps through the C ABI with HOST buffers: pinned TV in
+            through tg_mesh_create(tv_on_device = 0), the pinned field through
+            tg_critical_points(field_on_device = 0), every relation plus the
+            classes copied back to pinned host memory
+            (tg_copy_relations_async_i32: CSR offsets as int32, narrowed on the
+            device by one launch), all inside the timed window.  Steps
+            alternate between two streams and two sets of host buffers, so a
+            step's copies back overlap the next step's extraction (the host
+            link, not the kernels, bounds this number).
+  batch     the uneven 512-mesh batch (tet counts log-uniform in [2k, 400k]):
+            one batched pipeline run per step against the plain per-mesh loop,
+            both timed with CUDA events, and their ratio.
 
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
 (the path does not shard within a mesh); value = tets of all ranks / max time.
@@ -29,6 +40,7 @@ process per core, each step a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import functools
 import json
 import multiprocessing as mp
 import os
@@ -46,14 +58,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mtets/s (13 relations + crit. points), batched vs per-mesh on 1 GB300; p99 ms"
 UNIT = "Mtets/s"
-WORKLOAD = "kuhn64_coned20_irregular"
+WORKLOAD = "kuhn128_permuted_large"
 # --workload: the irregular single mesh (the headline), the 128^3 large mesh,
 # or the uneven 512-mesh batch (batched path against the per-mesh loop)
 WORKLOADS = {"irregular": "kuhn64_coned20_irregular", "large": "kuhn128_permuted_large",
              "batch": "batch512_uneven_2k_400k", "serve": "serve_poisson_70new_30field"}
-DEFAULT_STEPS = {"irregular": 300, "large": 60, "batch": 5, "serve": 1}
+DEFAULT_STEPS = {"irregular": 300, "large": 20, "batch": 5, "serve": 1}
 
 
+@functools.lru_cache(maxsize=2)
 def load_workload(key: str):
     from tetragpu_gb300 import meshgen
     return WORKLOADS[key], (meshgen.workload_irregular() if key == "irregular"
@@ -155,44 +168,38 @@ def output_bytes(counts: dict, totals: dict) -> int:
 
 
 def kernel_bytes(name: str, c: dict, tot: dict) -> int:
-    """One-touch bytes of one kernel's inputs and outputs (each array read or
-    written once), per launch.  k_star_b reads VT (4 B per entry), the sorted
-    TV (16 B per cell), pass A's three candidate masks (24 B per VT entry),
-    VT / VV offsets, the edge and face rank words and the ET / EF offsets; it
-    writes VV and the id-sorted incident edges (4 B each per VV entry), TE,
-    TF, FT's second cell, ET and EF."""
+    """Compulsory bytes one launch of a kernel is responsible for: the path's
+    inputs it reads once and the final outputs it writes once.  Intermediates
+    (pass A's candidate masks, the id-sorted incident edges, rank words,
+    offsets read back) are overhead and not credited.  k_star_b reads the
+    sorted TV (16 B per cell) and writes TE, TF, FT's second cell, the ET and
+    EF entries and the VV entries."""
     V, E, F, T = c["V"], c["E"], c["F"], c["T"]
     if name == "k_star_b":
-        reads = 4 * 4 * T + 16 * T + 24 * 4 * T + 8 * (V + 1) * 2 + 8 * ((6 * T + 31) // 32) \
-            + 8 * ((4 * T + 31) // 32) + 8 * (E + 1) * 2
-        writes = 4 * 2 * E * 2 + 4 * 6 * T + 4 * 4 * T + 4 * F + 4 * tot["ET"] + 4 * tot["EF"]
-        return reads + writes
-    if name == "k_star_a":
-        return 4 * 4 * T + 16 * T + 8 * (V + 1) + 24 * 4 * T + 4 * V + 2 * 6 * T \
-            + 2 * 4 * ((4 * T + 31) // 32) + 4 * ((6 * T + 31) // 32)
-    if name == "k_ee_fill":
-        return 8 * E + 4 * 2 * E + 8 * (E + 1) + 8 * (V + 1) + 4 * tot["EE"]
+        return 16 * T + 4 * 6 * T + 4 * 4 * T + 4 * F + 4 * tot["ET"] + 4 * tot["EF"] \
+            + 4 * tot["VV"]
     raise KeyError(name)
 
 
-def traffic_from_profiles(kernel: str, workload: str, scale: float):
-    """DRAM bytes per launch recorded from an ncu capture (profiles/*.md, a
-    line 'dram_bytes_per_launch: N' and 'cells: T'), scaled to this run."""
-    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+def traffic_from_profiles(name: str, workload: str, scale: float,
+                          key: str = "dram_bytes_per_launch"):
+    """DRAM bytes recorded from an ncu capture (profiles/<name>_<workload>.md,
+    a line '<key>: N' and a line 'cells: T'), scaled to this run's cells."""
+    p = os.path.join(ROOT, "profiles", f"{name}_{workload}.md")
     if not os.path.exists(p):
         return None
     vals = {}
     with open(p) as f:
         for line in f:
-            if ":" in line and line.strip().startswith(("dram_bytes_per_launch", "cells")):
+            if ":" in line and line.strip().startswith((key, "cells")):
                 k, v = line.split(":", 1)
                 try:
                     vals[k.strip()] = float(v.strip().split()[0].replace(",", ""))
                 except ValueError:
                     pass
-    if "dram_bytes_per_launch" not in vals:
+    if key not in vals:
         return None
-    b = vals["dram_bytes_per_launch"]
+    b = vals[key]
     if "cells" in vals and vals["cells"] > 0:
         b *= scale / vals["cells"]
     return int(b)
@@ -269,11 +276,12 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def main_batch(args, torch, dist, tg, rank, local_rank, world):
+def run_batch(args, torch, dist, tg, rank, local_rank, world, steps, e2e_steps):
     """The uneven 512-mesh batch: one batched pipeline run (tg_batch_*) per
     step against the plain per-mesh loop (tg_mesh_* per mesh) over the same
     device-resident meshes; both arms time the same step (create, all 13
-    relations, critical points, destroy) with CUDA events."""
+    relations, critical points, destroy) with CUDA events.  Returns the JSON
+    line's fields (rank 0)."""
     from tetragpu_gb300 import meshgen
     meshes = meshgen.workload_batch()
     nc = np.array([m.n_cells for m in meshes], dtype=np.int64)
@@ -330,11 +338,11 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
 
     clocks = Clocks(local_rank)
     clocks.start()
-    t_batch, launches = timed(batch_step, args.steps)
+    t_batch, launches = timed(batch_step, steps)
     clk = clocks.stop()
-    t_loop, loop_launches = timed(loop_step, args.steps)
-    value = world * args.steps * T / t_batch / 1e6
-    loop_value = world * args.steps * T / t_loop / 1e6
+    t_loop, loop_launches = timed(loop_step, steps)
+    value = world * steps * T / t_batch / 1e6
+    loop_value = world * steps * T / t_loop / 1e6
 
     # e2e: host TV and fields in, every relation of the union and the classes
     # back to pinned host memory, through the batch API.  As for the single
@@ -346,7 +354,7 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
     e2e_value, h2d, d2h = None, pin_tv.numel() * 4 + pin_f.numel() * 4, 12 * V
     lib = tg.load()
     C = tg._lib.C
-    if args.e2e_steps > 0:
+    if e2e_steps > 0:
         e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
         d_tv2 = [torch.empty_like(d_tv) for _ in range(2)]
         d_f2 = [torch.empty_like(d_f) for _ in range(2)]
@@ -401,14 +409,15 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
         d2h += sum(a.numel() * 4 + (bb.numel() * 4 if bb is not None else 0)
                    for a, bb in h_bufs[0].values())
         t0 = time.perf_counter()
-        e2e_run(args.e2e_steps)
-        e2e_value = round(world * args.e2e_steps * T / (time.perf_counter() - t0) / 1e6, 3)
+        e2e_run(e2e_steps)
+        e2e_value = round(world * e2e_steps * T / (time.perf_counter() - t0) / 1e6, 3)
 
+    line = None
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": max(3, args.warmup),
-            "ms_per_step": round(1e3 * t_batch / args.steps, 3), "higher_is_better": True,
+            "steps": steps, "warmup": max(3, args.warmup),
+            "ms_per_step": round(1e3 * t_batch / steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": WORKLOADS["batch"], "meshes": len(meshes), "cells": T,
                        "vertices": V, "relations": "all 13 + critical points",
@@ -417,12 +426,19 @@ def main_batch(args, torch, dist, tg, rank, local_rank, world):
             "gpu_launches": int(launches),
             "clocks": clk,
             "per_mesh_loop": {"value": round(loop_value, 3), "unit": UNIT,
-                              "ms_per_step": round(1e3 * t_loop / args.steps, 3),
+                              "ms_per_step": round(1e3 * t_loop / steps, 3),
                               "gpu_launches": int(loop_launches)},
             "batched_over_loop": round(value / loop_value, 3),
+            "tuning": tg.batch_tuning(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
         }
+    return line
+
+
+def main_batch(args, torch, dist, tg, rank, local_rank, world):
+    line = run_batch(args, torch, dist, tg, rank, local_rank, world, args.steps, args.e2e_steps)
+    if rank == 0:
         print(json.dumps(line), flush=True)
 
 
@@ -553,8 +569,10 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tetragpu", choices=["tetragpu", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--workload", default="irregular", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--batch-steps", type=int, default=3,
+                    help="timed steps of the 512-mesh batch leg beside the large mesh (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-rates", default="500,2000,8000,32000",
                     help="offered request rates (per second) for --workload serve")
@@ -564,7 +582,7 @@ def main():
         args.steps = 20 if args.impl == "reference" else DEFAULT_STEPS[args.workload]
     if args.impl == "reference":
         if args.workload in ("batch", "serve"):
-            args.workload = "irregular"
+            args.workload = "large"
         run_reference(args)
         return
 
@@ -577,7 +595,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
 
     import tetragpu_gb300 as tg
-    from tetragpu_gb300 import _build, meshgen
+    from tetragpu_gb300 import _build
     if not os.path.exists(_build.LIB):
         _build.build()
     tg.load()
@@ -592,14 +610,40 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
+    line = run_single(args, torch, dist, tg, rank, local_rank, world)
+    if args.workload == "large" and args.batch_steps > 0:
+        b = run_batch(args, torch, dist, tg, rank, local_rank, world, args.batch_steps, 0)
+        if rank == 0:
+            line["batch"] = {
+                "workload": b["config"]["workload"], "meshes": b["config"]["meshes"],
+                "cells": b["config"]["cells"], "value": b["value"], "unit": UNIT,
+                "ms_per_step": b["ms_per_step"], "steps": b["steps"],
+                "gpu_launches": b["gpu_launches"], "per_mesh_loop": b["per_mesh_loop"],
+                "batched_over_loop": b["batched_over_loop"], "tuning": b["tuning"],
+                "clocks": b["clocks"]}
+            line["gpu_launches_batch_leg"] = b["gpu_launches"] + \
+                b["per_mesh_loop"]["gpu_launches"]
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            _, mesh = load_workload(args.workload)
+            line["cpu_baseline"] = cpu_baseline(mesh, line["config"]["workload"])
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_single(args, torch, dist, tg, rank, local_rank, world):
+    """One mesh per step (device-resident value, host-buffer e2e); returns the
+    JSON line (rank 0) without the CPU baseline."""
     workload, mesh = load_workload(args.workload)
     T, V = mesh.n_cells, mesh.n_verts
+    dev = f"cuda:{local_rank}"
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
-    d_tv = torch.from_numpy(mesh.tv).to(f"cuda:{local_rank}")
-    d_field = torch.from_numpy(mesh.field).to(f"cuda:{local_rank}")
-    d_classes = torch.empty(3 * V, dtype=torch.int32, device=f"cuda:{local_rank}")
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local_rank}")
+    d_tv = torch.from_numpy(mesh.tv).to(dev)
+    d_field = torch.from_numpy(mesh.field).to(dev)
+    d_classes = torch.empty(3 * V, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
 
     def step():
@@ -648,84 +692,77 @@ def main():
     total_s = sum(ms) / 1e3
     t_max = total_s
     if world > 1:
-        t_max = max_over_ranks(total_s, dist, torch, f"cuda:{local_rank}")
+        t_max = max_over_ranks(total_s, dist, torch, dev)
         dist.barrier()
     value = world * args.steps * T / t_max / 1e6
 
     # ---- e2e: host buffers through the C ABI ----
-    # Each step: pinned TV and field in, every relation and the classes out to
-    # pinned host memory.  Steps alternate between two streams and two sets
-    # of host buffers, so one step's copies back (host-link bound) overlap the
-    # next step's extraction, the way a caller processing many meshes would
-    # run; the timed region covers every copy of every step.
+    # Each step: tg_mesh_create from the pinned host TV (the library copies it
+    # in), tg_extract, tg_critical_points from the pinned host field (copied
+    # in by the library) into device classes, then every relation and the
+    # classes out to pinned host memory.  Steps alternate between two streams
+    # and two sets of host buffers, so one step's copies back (host-link
+    # bound) overlap the next step's extraction, the way a caller processing
+    # many meshes would run; the timed region covers every copy of every step.
     pin_tv = torch.from_numpy(mesh.tv).pin_memory()
     pin_field = torch.from_numpy(mesh.field).pin_memory()
     names = tg.RELATIONS[1:]
     fixed_rows = {"TE": (Tc, 6), "EV": (E, 2), "TF": (Tc, 4), "FV": (F, 3), "FE": (F, 3),
                   "FT": (F, 2)}
     csr_rows = {"ET": E, "EF": E, "VT": Vc, "TT": Tc, "FF": F, "EE": E, "VV": Vc}
-    bufs = []
-    for _ in range(2):
-        h_ent = {n: torch.empty(max(r * w, 1), dtype=torch.int32).pin_memory()
-                 for n, (r, w) in fixed_rows.items()}
-        h_ent.update({n: torch.empty(max(totals[n], 1), dtype=torch.int32).pin_memory()
-                      for n in csr_rows})
-        h_off = {n: torch.empty(r + 1, dtype=torch.int32).pin_memory() for n, r in csr_rows.items()}
-        h_cls = torch.empty(3 * V, dtype=torch.int32).pin_memory()
-        bufs.append((h_ent, h_off, h_cls))
-    ptr_off, ptr_ent = [], []
-    for h_ent, h_off, _ in bufs:
-        po, pe = (tg._lib.C.c_void_p * 14)(), (tg._lib.C.c_void_p * 14)()
-        for n in names:
-            pe[tg.REL[n]] = h_ent[n].data_ptr()
-            if n in h_off:
-                po[tg.REL[n]] = h_off[n].data_ptr()
-        ptr_off.append(po)
-        ptr_ent.append(pe)
-    h2d = pin_tv.numel() * 4 + pin_field.numel() * 4
-    d2h = sum(r * w * 4 for r, w in fixed_rows.values()) + sum(totals[n] * 4 for n in csr_rows) \
-        + sum((r + 1) * 4 for r in csr_rows.values()) + V * 12
     lib = tg.load()
-    dev = f"cuda:{local_rank}"
-    e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
-    d_cls2 = [torch.empty(3 * V, dtype=torch.int32, device=dev) for _ in range(2)]
-    d_tv2 = [torch.empty_like(d_tv) for _ in range(2)]
-    d_f2 = [torch.empty_like(d_field) for _ in range(2)]
-
-    def upload(k):
-        # a step's inputs go up before the previous step's results come down:
-        # the copies share one queue, so an upload behind them would wait
-        with torch.cuda.stream(e_streams[k % 2]):
-            d_tv2[k % 2].copy_(pin_tv, non_blocking=True)
-            d_f2[k % 2].copy_(pin_field, non_blocking=True)
-
-    def e2e_run(n_steps):
-        live = None
-        upload(0)
-        for k in range(n_steps):
-            es = e_streams[k % 2].cuda_stream
-            h_ent, h_off, h_cls = bufs[k % 2]
-            g = tg.Mesh(d_tv2[k % 2].data_ptr(), V, n_cells=T, on_device=True, stream=es)
-            g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=es)
-            tg._lib.check(lib.tg_critical_points(g._h, d_f2[k % 2].data_ptr(), tg.FIELD_F32, 1,
-                                                 d_cls2[k % 2].data_ptr(), 1, es))
-            if k + 1 < n_steps:
-                upload(k + 1)
-            # every relation through one call: CSR offsets narrowed to int32
-            # by one launch, then the copies back to back
-            tg._lib.check(lib.tg_copy_relations_async_i32(g._h, tg.ALL_RELATIONS,
-                                                          ptr_off[k % 2], ptr_ent[k % 2], es))
-            with torch.cuda.stream(e_streams[k % 2]):
-                h_cls.copy_(d_cls2[k % 2], non_blocking=True)
-            if live is not None:
-                live.close()        # waits for the previous step's copies
-            live = g
-        if live is not None:
-            live.close()
-        torch.cuda.synchronize()
-
-    e2e_value = None
+    Cc = tg._lib.C
+    e2e_value, h2d, d2h = None, 0, 0
     if args.e2e_steps > 0:
+        bufs = []
+        for _ in range(2):
+            h_ent = {n: torch.empty(max(r * w, 1), dtype=torch.int32).pin_memory()
+                     for n, (r, w) in fixed_rows.items()}
+            h_ent.update({n: torch.empty(max(totals[n], 1), dtype=torch.int32).pin_memory()
+                          for n in csr_rows})
+            h_off = {n: torch.empty(r + 1, dtype=torch.int32).pin_memory()
+                     for n, r in csr_rows.items()}
+            h_cls = torch.empty(3 * V, dtype=torch.int32).pin_memory()
+            bufs.append((h_ent, h_off, h_cls))
+        ptr_off, ptr_ent = [], []
+        for h_ent, h_off, _ in bufs:
+            po, pe = (Cc.c_void_p * 14)(), (Cc.c_void_p * 14)()
+            for n in names:
+                pe[tg.REL[n]] = h_ent[n].data_ptr()
+                if n in h_off:
+                    po[tg.REL[n]] = h_off[n].data_ptr()
+            ptr_off.append(po)
+            ptr_ent.append(pe)
+        h2d = pin_tv.numel() * 4 + pin_field.numel() * 4
+        d2h = sum(r * w * 4 for r, w in fixed_rows.values()) + \
+            sum(totals[n] * 4 for n in csr_rows) + sum((r + 1) * 4 for r in csr_rows.values()) + \
+            V * 12
+        e_streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        d_cls2 = [torch.empty(3 * V, dtype=torch.int32, device=dev) for _ in range(2)]
+
+        def e2e_run(n_steps):
+            live = None
+            for k in range(n_steps):
+                es = e_streams[k % 2].cuda_stream
+                h_ent, h_off, h_cls = bufs[k % 2]
+                h = Cc.c_void_p()
+                tg._lib.check(lib.tg_mesh_create(pin_tv.data_ptr(), T, V, 0, es, Cc.byref(h)))
+                tg._lib.check(lib.tg_extract(h, tg.ALL_RELATIONS, tg.OPT_LINK_ADJACENCY, es))
+                tg._lib.check(lib.tg_critical_points(h, pin_field.data_ptr(), tg.FIELD_F32, 0,
+                                                     d_cls2[k % 2].data_ptr(), 1, es))
+                # every relation through one call: CSR offsets narrowed to
+                # int32 by one launch, then the copies back to back
+                tg._lib.check(lib.tg_copy_relations_async_i32(h, tg.ALL_RELATIONS,
+                                                              ptr_off[k % 2], ptr_ent[k % 2], es))
+                with torch.cuda.stream(e_streams[k % 2]):
+                    h_cls.copy_(d_cls2[k % 2], non_blocking=True)
+                if live is not None:
+                    lib.tg_mesh_destroy(live)   # waits for the previous step's copies
+                live = h
+            if live is not None:
+                lib.tg_mesh_destroy(live)
+            torch.cuda.synchronize()
+
         e2e_run(2)
         if world > 1:
             dist.barrier()
@@ -733,43 +770,49 @@ def main():
         e2e_run(args.e2e_steps)
         e2e_s = time.perf_counter() - t0
         if world > 1:
-            e2e_s = max_over_ranks(e2e_s, dist, torch, f"cuda:{local_rank}")
+            e2e_s = max_over_ranks(e2e_s, dist, torch, dev)
         e2e_value = round(world * args.e2e_steps * T / e2e_s / 1e6, 3)
 
-    if rank == 0:
-        peak, peak_kind = peaks()
-        kb = kernel_bytes(ROOFLINE_KERNEL, counts, totals)
-        per_launch_s = (kern_ms / 1e3) / max(kern_n, 1)
-        achieved = kb / per_launch_s / 1e9 if kern_n else None
-        traffic = traffic_from_profiles(ROOFLINE_KERNEL, workload, T)
-        alg = output_bytes(counts, totals)
-        line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": max(3, args.warmup),
-            "ms_per_step": round(1e3 * t_max / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": workload, "cells": T, "vertices": V, "edges": E, "faces": F,
-                       "relations": "all 13 + critical points", "parallelism": f"replicas{world}",
-                       "l2": "flushed before every step (512 MB write)",
-                       "path_bytes_per_step": alg,
-                       "path_gbs_of_measured_peak": round(alg / (t_max / args.steps) / 1e9 / peak, 4)},
-            "gpu_launches": int(launches),
-            "wall_s": round(wall, 3),
-            "clocks": clk,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps},
-            "roofline": {"bound": "hbm", "kernel": ROOFLINE_KERNEL,
-                         "achieved": round(achieved, 1) if achieved else None, "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": kb,
-                         "launch_ms": round(per_launch_s * 1e3, 4), "launches": kern_n,
-                         "traffic": traffic},
-        }
-        if not args.no_cpu_baseline and world >= 1:
-            line["cpu_baseline"] = cpu_baseline(mesh, workload)
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    if rank != 0:
+        return None
+    peak, peak_kind = peaks()
+    step_s = t_max / args.steps
+    alg = output_bytes(counts, totals)
+    path_gbs = alg / step_s / 1e9
+    kb = kernel_bytes(ROOFLINE_KERNEL, counts, totals)
+    per_launch_s = (kern_ms / 1e3) / max(kern_n, 1)
+    k_gbs = kb / per_launch_s / 1e9 if kern_n else None
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": round(1e3 * step_s, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": workload, "cells": T, "vertices": V, "edges": E, "faces": F,
+                   "relations": "all 13 + critical points", "parallelism": f"replicas{world}",
+                   "l2": "flushed before every step (512 MB write)",
+                   "step": "tg_mesh_create + tg_extract(all 13, link adjacency) + "
+                           "tg_critical_points + tg_mesh_destroy"},
+        "gpu_launches": int(launches),
+        "wall_s": round(wall, 3),
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+                "path": "C ABI with host buffers: tg_mesh_create(host TV), tg_extract, "
+                        "tg_critical_points(host field), tg_copy_relations_async_i32"},
+        "roofline": {
+            "bound": "hbm", "scope": "path (one step: every kernel of create + extract + "
+                                     "critical points)",
+            "achieved": round(path_gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(path_gbs / peak, 4), "peak_source": peak_kind,
+            "algorithmic_bytes_per_step": alg,
+            "traffic": traffic_from_profiles("path", workload, T, "dram_bytes_per_step"),
+            "kernel": {"name": ROOFLINE_KERNEL, "achieved": round(k_gbs, 1) if k_gbs else None,
+                       "frac": round(k_gbs / peak, 4) if k_gbs else None,
+                       "algorithmic_bytes_per_launch": kb,
+                       "launch_ms": round(per_launch_s * 1e3, 4), "launches": kern_n,
+                       "traffic": traffic_from_profiles(ROOFLINE_KERNEL, workload, T)},
+        },
+    }
 
 
 if __name__ == "__main__":

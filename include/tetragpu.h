@@ -98,6 +98,10 @@ typedef struct tg_mesh tg_mesh;
 /* Library version string. */
 const char *tg_version(void);
 
+/* The tile parameters the kernels use (window sizes of the star passes and
+ * of the link adjacency), as a JSON object. */
+const char *tg_tuning_info(void);
+
 /* Description of the last error on this thread ("" if none). */
 const char *tg_last_error_string(void);
 
@@ -215,23 +219,25 @@ int64_t tg_mesh_device_bytes(const tg_mesh *mesh);
 /* Number of kernel launches this library has issued in this process. */
 int64_t tg_kernel_launch_count(void);
 
-/* Critical points for callers that cannot allocate device memory: code
- * running while a stream is being captured (no cudaMalloc there), a host
- * application that gives this library a fixed memory budget up front, a
- * real-time loop that forbids allocator calls after start-up.  No
- * counterpart in the reference.  Inputs and output are device memory the
- * caller owns: VV as CSR (vv_off [n_verts + 1], vv [n_vv_entries], rows
- * sorted, as tg_get_relation returns it), the field (TG_FIELD_F32/F64,
- * n_verts values) and classes_out (uint32 [n_verts x 3], the layout of
- * tg_critical_points).  The link adjacency goes to a fixed device array of
- * TG_NOALLOC_MAX_VV_ENTRIES 64-bit masks (64 MiB, plus a 128 KiB window table)
- * that every GPU loading the library holds until the process exits; larger VV
- * is rejected with
- * TG_ERR_UNSUPPORTED.  The first call on a device looks up that array's
- * device address, so make it before any stream capture begins.  Calls share
- * the array: calls that overlap on the GPU race, so serialise them.  The
- * call waits for its stream to read the kernels' status word.  Nothing is
- * allocated (no cudaMalloc, cudaFree or allocating library routine). */
+/* Critical points for callers that cannot allocate device memory when they
+ * classify: a host application that gives this library a fixed device-memory
+ * budget at start-up and accounts for every byte afterwards, or a real-time
+ * loop whose rules forbid allocator calls (and the synchronisation they can
+ * bring) once it runs.  No counterpart in the reference.  Inputs and output
+ * are device memory the caller owns: VV as CSR (vv_off [n_verts + 1], vv
+ * [n_vv_entries], rows sorted, as tg_get_relation returns it), the field
+ * (TG_FIELD_F32/F64, n_verts values) and classes_out (uint32 [n_verts x 3],
+ * the layout of tg_critical_points).  The link adjacency goes to a fixed
+ * device array of TG_NOALLOC_MAX_VV_ENTRIES 64-bit masks (64 MiB, plus a
+ * 128 KiB window table) that every GPU loading the library holds until the
+ * process exits; larger VV is rejected with TG_ERR_UNSUPPORTED before
+ * anything runs, and so is a vertex with more than 64 neighbours (after the
+ * kernels ran: classes_out is then not valid).  The first call on a device
+ * looks up that array's device address.  Calls share the array and keep the
+ * last call's contents in it: calls that overlap on the GPU race, so
+ * serialise them.  The call reads the kernels' status word back, so it
+ * waits for its stream before returning.  Nothing is allocated (no
+ * cudaMalloc, cudaFree or allocating library routine). */
 #define TG_NOALLOC_MAX_VV_ENTRIES (1 << 23)
 tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int32_t *vv, int64_t n_verts,
                                      int64_t n_vv_entries, const void *field, int field_type,

@@ -11,9 +11,12 @@
 #     defined (the configure step of CMakeLists.txt:15-19).
 # Everything is written under oracle/_ref/, which git ignores.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $TG_REFERENCE_ROOT, else /root/reference.
+# Exits 2 when the tree is absent.  The root it used is recorded in
+# oracle/_ref/reference_root for the tests that compile against its headers.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${TG_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/cpu_extraction.cpp" ]; then
@@ -43,4 +46,5 @@ for src in "$REF/src/cpu_extraction.cpp" "$REF/src/validate.cpp" "$REF/src/metri
 done
 wait
 $CXX -shared -o "$OUT/libtgref.so" "${objs[@]}"
+printf '%s\n' "$(cd "$REF" && pwd)" > "$OUT/reference_root"
 echo "built $OUT/libtgref.so"

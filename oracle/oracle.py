@@ -56,13 +56,31 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
-    """Compile the reference's CPU code if its source tree is present."""
-    if not os.path.isfile(os.path.join(ref_root, "src", "cpu_extraction.cpp")):
+def build_reference(ref_root: str | None = None) -> str | None:
+    """Compile the reference's CPU code if its source tree is present.
+
+    The tree is ``ref_root`` when given, else the ``TG_REFERENCE_ROOT``
+    environment variable, else build_ref.sh's own default.  Returns None when
+    no tree is found (the tests that need it skip)."""
+    cmd = [os.path.join(HERE, "build_ref.sh")]
+    if ref_root:
+        cmd.append(ref_root)
+    r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+    if r.returncode == 2:
         return None
-    subprocess.check_call([os.path.join(HERE, "build_ref.sh"), ref_root],
-                          stdout=subprocess.DEVNULL)
+    if r.returncode != 0:
+        raise RuntimeError("build_ref.sh failed:\n" + r.stderr)
     return REF_LIB
+
+
+def reference_root() -> str | None:
+    """The reference source tree the last build_reference() compiled, if any."""
+    p = os.path.join(HERE, "_ref", "reference_root")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        root = f.read().strip()
+    return root if os.path.isdir(root) else None
 
 
 def _i32(a):

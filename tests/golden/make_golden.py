@@ -38,9 +38,10 @@ def cases():
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # the reference tree: argv[1], else TG_REFERENCE_ROOT, else build_ref.sh's default
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else None
     if O.build_reference(ref_root) is None:
-        sys.exit(f"reference source tree not found at {ref_root}")
+        sys.exit("reference source tree not found (pass it or set TG_REFERENCE_ROOT)")
     O.build()
     orc = O.Oracle()
     ref = O.Reference()

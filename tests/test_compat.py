@@ -26,13 +26,13 @@ def test_signatures_match_reference_headers(tmp_path):
     """The reference's datatypes.h + cuda_extraction.h and tetragpu_compat.h
     compile together (same signatures) and every entry point links."""
     from oracle import oracle as O
-    if O.build_reference() is None:
-        pytest.skip("reference source tree not present")
+    if O.build_reference() is None or O.reference_root() is None:
+        pytest.skip("reference source tree not present (TG_REFERENCE_ROOT)")
     from tetragpu_gb300 import _build
     _build.build()
     out = tmp_path / "sig"
     cmd = [_nvcc(), "-std=c++17", "-I", os.path.join(ROOT, "oracle", "_ref", "include"),
-           "-I", "/root/reference/include", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(O.reference_root(), "include"), "-I", os.path.join(ROOT, "include"),
            os.path.join(HERE, "signatures.cu"), "-o", str(out),
            "-L", os.path.dirname(_build.LIB), "-ltetragpu",
            "-Xlinker", "-rpath=" + os.path.dirname(_build.LIB)]

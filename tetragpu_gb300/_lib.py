@@ -73,6 +73,7 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_critical_points": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]),
         "tg_mesh_device_bytes": (i64, [vp]),
         "tg_kernel_launch_count": (i64, []),
+        "tg_tuning_info": (C.c_char_p, []),
         "tg_profile_kernel": (C.c_int, [C.c_char_p]),
         "tg_profile_read": (C.c_int, [P(C.c_double), P(i64), C.c_int]),
         "tg_batch_create": (C.c_int, [vp, vp, vp, i64, C.c_int, vp, P(vp)]),
@@ -474,6 +475,21 @@ def profile_read(reset: bool = True) -> tuple:
     ms, n = C.c_double(), C.c_int64()
     check(load().tg_profile_read(C.byref(ms), C.byref(n), int(reset)))
     return ms.value, n.value
+
+
+def tuning_info() -> dict:
+    """The tile parameters the kernels use (tg_tuning_info)."""
+    import json
+    return json.loads(load().tg_tuning_info().decode())
+
+
+def batch_tuning() -> dict:
+    """How the batched path is tuned: the batch runs as one disjoint-union
+    mesh, so every kernel launches once with the tiles below, whatever the
+    sizes of its members."""
+    d = tuning_info()
+    d["selection"] = "one setting for every batch (the union's windows do not depend on member sizes)"
+    return d
 
 
 def version() -> str:

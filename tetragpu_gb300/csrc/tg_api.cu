@@ -717,7 +717,21 @@ tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const voi
 
 extern "C" {
 
-const char *tg_version(void) { return "tetragpu-gb300 1.0 (sm_103a)"; }
+const char *tg_version(void) { return "tetragpu-gb300 1.1 (sm_103a)"; }
+
+const char *tg_tuning_info(void)
+{
+    static std::string info;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "{\"star_a_window\": %d, \"star_b_window\": %d, \"adjacency_window\": %d}",
+                 star_window(), star_window_b(), crit_window());
+        info = buf;
+    });
+    return info.c_str();
+}
 
 const char *tg_last_error_string(void) { return g_err.c_str(); }
 

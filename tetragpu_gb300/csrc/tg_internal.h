@@ -37,6 +37,14 @@ enum StatusFlag : unsigned int {
 constexpr int kMaxStar = 64;
 constexpr int kMaxDeg = 64;
 
+// VV entries per window of the link-adjacency kernel (tg_crit.cu): its
+// window table has n_vv / kAdjWin + 2 entries
+#ifndef TG_ADJ_WIN
+#define TG_ADJ_WIN 256
+#endif
+constexpr int kAdjWin = TG_ADJ_WIN;
+static_assert(kAdjWin >= 64 && kAdjWin <= 4096, "link-adjacency window size");
+
 // ---- scans (tg_scan.cu) ----
 enum ScanKind : int {
     SCAN_COUNT_I32 = 0,  // in: int32 counts, out: int64 offsets [n + 1]

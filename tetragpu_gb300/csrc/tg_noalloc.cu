@@ -2,14 +2,16 @@
 //
 // tg_critical_points builds the link adjacency of every vertex (one 64-bit
 // mask per VV entry) in memory it allocates and caches on the mesh.  Some
-// callers cannot allocate at that point: code that runs while a CUDA stream
-// is being captured (cudaMalloc is not allowed there), host applications
-// that hand a fixed memory budget to a plugin up front, or real-time loops
-// that forbid allocator calls after start-up.  tg_critical_points_noalloc
-// serves them: the caller passes VV (device CSR), the field and the output,
-// and the adjacency lives in file-scope device arrays of fixed size,
-// TG_NOALLOC_MAX_VV_ENTRIES masks (64 MiB) plus their window table (128 KiB),
-// which every GPU that loads this library holds until the process exits.
+// callers cannot allocate device memory when they classify: a host
+// application that hands this library a fixed device-memory budget at
+// start-up and accounts for every byte afterwards, or a real-time loop whose
+// rules forbid allocator calls (and the synchronisation they can cause) once
+// it runs.  tg_critical_points_noalloc serves them: the caller passes VV
+// (device CSR), the field and the output, and the adjacency lives in
+// file-scope device arrays of fixed size, TG_NOALLOC_MAX_VV_ENTRIES masks
+// (64 MiB) plus their window table (128 KiB), which every GPU that loads
+// this library holds until the process exits.  The call reads the kernels'
+// status word back and waits for its stream to do so.
 #include <climits>
 #include <cstdio>
 #include <mutex>
@@ -23,8 +25,8 @@ namespace {
 // word for the kernels.  Calls that overlap on the GPU (two streams at once)
 // race on it; serialise them.
 static __device__ __align__(256) unsigned long long g_noalloc_adj[TG_NOALLOC_MAX_VV_ENTRIES];
-static __device__ __align__(256) int g_noalloc_win[TG_NOALLOC_MAX_VV_ENTRIES / 256 + 2];
-// (the window table of the adjacency kernel: 256-entry windows over VV)
+// (the window table of the adjacency kernel: kAdjWin-entry windows over VV)
+static __device__ __align__(256) int g_noalloc_win[TG_NOALLOC_MAX_VV_ENTRIES / tg::kAdjWin + 2];
 static __device__ __align__(256) tg::DevStatus g_noalloc_status;
 
 constexpr int kMaxDevices = 64;
@@ -95,7 +97,11 @@ extern "C" tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int
     void *adj = nullptr, *win = nullptr, *status = nullptr;
     tg_status st = scratch_for_current_device(&adj, &win, &status);
     if (st != TG_OK) return st;
+    static_assert(tg::kAdjWin >= 1, "window size");
     cudaStream_t s = (cudaStream_t)stream;
+    // an error left by an earlier, unrelated call would be reported as this
+    // call's: clear it (sticky errors come back from the calls below)
+    (void)cudaGetLastError();
     // the status word keeps the previous call's contents: clear it; the
     // window table and every adjacency mask are rewritten before they are read
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(tg::DevStatus), s);
@@ -105,11 +111,19 @@ extern "C" tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int
                         (tg::DevStatus *)status, s);
     tg::launch_crit_classify(vv_off, vv, (const uint64_t *)adj, field, field_type, 0, n_verts,
                              classes_out, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TG_ERR_CUDA, "launching the critical-point kernels", e);
     tg::DevStatus out{};
     e = cudaMemcpyAsync(&out, status, sizeof out, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(TG_ERR_CUDA, "critical-point kernels", e);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(TG_ERR_CUDA, "critical-point kernels", e);
+    }
+    // a row longer than the 64-bit link masks hold: its masks were not
+    // written, so the classes of that call are not valid
     if (out.flags & tg::ST_HEAVY_DEG)
-        return fail(TG_ERR_UNSUPPORTED, "a vertex has more than 64 neighbours");
+        return fail(TG_ERR_UNSUPPORTED,
+                    "a vertex has more than 64 neighbours (tg_critical_points handles it)");
     return TG_OK;
 }
