@@ -160,16 +160,31 @@ def _fan(n_tets):
 
 
 @pytest.mark.parametrize("n_tets", [70, 30])
-def test_beyond_star_limits_is_unsupported(gpu_lib, oracle, n_tets):
-    # 70 cells around a vertex exceed the 64-cell star; 30 give 90 neighbours,
-    # beyond the 64 a link mask holds.  Both are refused with a status, and
-    # the device stays usable.
+def test_beyond_fast_path_limits_bit_exact(gpu_lib, oracle, n_tets):
+    """70 cells around a vertex exceed the star passes' 64-cell masks (the
+    heavy-star path takes it); 30 give 90 neighbours, beyond the 64 a link
+    mask holds (the heavy EE and critical-point paths).  Every relation and
+    the classes against the oracle, alone and inside a coned grid (the
+    reference has no such bound, src/cpu_extraction.cpp:259-289)."""
     tv, nv = _fan(n_tets)
-    with gpu_lib.Mesh(tv, nv) as g:
-        with pytest.raises(gpu_lib.TetraGPUError) as ei:
-            g.extract(gpu_lib.ALL_RELATIONS)
-        assert ei.value.code == 5
-    _check_mesh(gpu_lib, oracle, meshgen.kuhn_mesh(2, 0.5, seed=3))
+    rng = np.random.default_rng(n_tets)
+    m = meshgen.Mesh(tv=tv, n_verts=nv, coords=np.zeros((nv, 3), np.float32), name="fan")
+    _check_mesh(gpu_lib, oracle, m)
+    grid = meshgen.kuhn_mesh(4, 0.3, seed=3)
+    perm = rng.permutation(grid.n_verts + nv).astype(np.int32)
+    both_tv = perm[np.concatenate([tv + grid.n_verts, grid.tv])]
+    both = meshgen.Mesh(tv=both_tv, n_verts=grid.n_verts + nv,
+                        coords=np.zeros((grid.n_verts + nv, 3), np.float32), name="fan+grid")
+    _check_mesh(gpu_lib, oracle, both)
+    field = rng.standard_normal(both.n_verts).astype(np.float32)
+    tvs = oracle.canonicalize(both.tv, both.n_verts)
+    with gpu_lib.Mesh(both.tv, both.n_verts) as g:
+        assert np.array_equal(g.critical_points(field),
+                              oracle.critical_points(tvs, both.n_verts, field))
+    with gpu_lib.Mesh(both.tv, both.n_verts) as g:   # adjacency built during the extraction
+        g.extract(gpu_lib.ALL_RELATIONS, options=gpu_lib.OPT_LINK_ADJACENCY)
+        assert np.array_equal(g.critical_points(-field),
+                              oracle.critical_points(tvs, both.n_verts, -field))
 
 
 def test_large_mesh_properties(gpu_lib):

@@ -336,6 +336,8 @@ struct tg_mesh {
     int32_t *vtp = nullptr;             // [4T] VT rows in that order
     int32_t *st_win = nullptr;          // window table over pofs (star pass A)
     int32_t *st_win_b = nullptr;        // the same for star pass B's windows
+    int32_t *st_wbase = nullptr;        // first entry of each pass A window
+    int32_t *st_wbase_b = nullptr;      // first entry of each pass B window
     ScanWorkspace scan;                 // every prefix scan of the mesh (tg_scan.cu)
     // segments of cells (the meshes of a batch): cell starts, and after each
     // extraction their first edge and face ids (device, n_seg + 1 each)
@@ -343,6 +345,10 @@ struct tg_mesh {
     int64_t *seg_c = nullptr;
     int64_t *seg_ef = nullptr;
     Rel rel[14];
+    // stars of more than kMaxStar cells (tg_heavy.cu): processing positions
+    // n_light .. n_light + n_heavy - 1, heavy_entries VT entries in all
+    int64_t n_light = 0, n_heavy = 0, heavy_entries = 0;
+    int max_deg = 0;            // largest degree above kMaxDeg seen by the extraction, else 0
     uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
     DevStatus *st = nullptr;    // device
     DevStatus *st_host = nullptr;
@@ -465,7 +471,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         const int64_t nwe = (6 * T + 31) / 32, nwf = (4 * T + 31) / 32;
         uint32_t *eflag, *fflag, *fbnd;
         uint2 *erank, *frank, *brank;
-        uint16_t *ecnt = nullptr;
+        uint32_t *ecnt = nullptr;
         int32_t *deg;
         int64_t *vv_off;
         const bool need_ecnt = mask & (TG_ET | TG_EF | TG_EE);
@@ -493,14 +499,32 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         TRY(tmp.alloc(&deg_sq, V + 1));
         uint64_t *emask;  // pass A's candidate masks, pass B's input
         TRY(tmp.alloc(&emask, 3 * NVT));
-        StarA a{m->pofs, m->st_win, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt, eflag, fflag,
-                fbnd, m->st, emask};
+        StarA a{m->pofs, m->st_win, m->st_wbase, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt,
+                eflag, fflag, fbnd, m->st, emask};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));
             a.ecnt = ecnt;
         }
         launch_star_a(a, s);
+        HeavyStars hv{};
+        if (m->n_heavy > 0) {
+            hv.n_light = m->n_light;
+            hv.n_heavy = m->n_heavy;
+            hv.pofs = m->pofs;
+            hv.vorder = m->vorder;
+            hv.vtp = m->vtp;
+            hv.tvs = m->tvs;
+            hv.st = m->st;
+            TRY(tmp.alloc(&hv.pairs, 3 * m->heavy_entries));
+            TRY(tmp.alloc(&hv.ids, 6 * m->heavy_entries));
+            hv.deg = deg;
+            hv.ecnt = a.ecnt;
+            hv.eflag = eflag;
+            hv.fflag = fflag;
+            hv.fbnd = fbnd;
+            launch_heavy_a(hv, s);
+        }
         ScanJob jobs[5] = {{deg, vv_off, V, SCAN_COUNT_I32, 0},
                            {eflag, erank, nwe, SCAN_POPC_RANK, 0},
                            {fflag, frank, nwf, SCAN_POPC_RANK, 0},
@@ -517,6 +541,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             TRY(sync_read(m, s, 5, src, w8));
         }
         if (m->st_host->flags) return check_flags(m);
+        m->max_deg = m->st_host->max_deg > kMaxDeg ? m->st_host->max_deg : 0;
         const int64_t nvv = m->sz_host[0];
         const int64_t E = m->sz_host[1], F = m->sz_host[2];
         const int64_t n_bnd = m->sz_host[3];  // boundary faces
@@ -551,7 +576,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (fv || ft || ff_off)
             launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, side.fork());
         if (et_off || ef_off || ee_off || ev) {
-            uint32_t *len;
+            uint2 *len;
             TRY(tmp.alloc(&len, E));
             launch_edge_offsets(eflag, ecnt, m->tvs, deg, erank, 6 * T, E, et_off, ef_off, ee_off,
                                 ev, len, m->scan, m->st, s);
@@ -581,7 +606,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             if (T == 0) CK(cudaMemsetAsync(ff_off, 0, 8, s));
         }
         StarB b{};
-        b.pofs = m->pofs; b.win = m->st_win_b; b.vorder = m->vorder; b.vtp = m->vtp;
+        b.pofs = m->pofs; b.win = m->st_win_b; b.wbase = m->st_wbase_b; b.vorder = m->vorder;
+        b.vtp = m->vtp;
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
@@ -589,6 +615,21 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
         side.join();
         launch_star_b(b, s);
+        if (m->n_heavy > 0) {
+            hv.vv_off = vv_off;
+            hv.erank = erank;
+            hv.frank = frank;
+            hv.vv = vv;
+            hv.eid_sorted = eid_sorted;
+            hv.te = te;
+            hv.tf = tf;
+            hv.ft = ft;
+            hv.et = et;
+            hv.ef = ef;
+            hv.et_off = et_off;
+            hv.ef_off = ef_off;
+            launch_heavy_b(hv, s);
+        }
         tmp.keep(vv);
         tmp.keep(vv_off);
         set_csr(m, TG_REL_VV, vv_off, vv, V, nvv);
@@ -615,10 +656,14 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
             if (prep_adj) {
                 launch_window_starts(vv_off, V, nvv, crit_window(), vv_win, s2);
-                launch_crit_adj(vv_off, vv, vv_win, V, nvv, m->cadj, m->st, s2);
+                launch_crit_adj(vv_off, vv, vv_win, V, nvv, m->cadj, m->st, m->max_deg ? 1 : 0,
+                                s2);
             }
         }
-        if (ee_off) launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+        if (ee_off) {
+            launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+            if (m->max_deg) launch_ee_heavy(ev, E, vv_off, eid_sorted, ee_off, ee, s);
+        }
         side.join();
         CK(cudaGetLastError());
 
@@ -692,7 +737,8 @@ tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const voi
         launch_window_starts(vv.off, V, vv.entries, crit_window(), vv_win, s);
         // VV rows longer than the adjacency masks were already rejected by
         // tg_extract (star pass A flags them), so no status read-back here
-        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st, s);
+        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st,
+                        m->max_deg ? 1 : 0, s);
         cudaFreeAsync(vv_win, s);
     }
     Temps tmp(s);
@@ -707,6 +753,17 @@ tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const voi
     uint32_t *out = classes_out;
     if (!out_on_device) TRY(tmp.alloc(&out, 3 * nv));
     launch_crit_classify(vv.off, vv.ent, m->cadj, f, field_type, v0, nv, out, s);
+    if (m->max_deg) {
+        // vertices of more than kMaxDeg neighbours: at most one per
+        // kMaxDeg + 1 VV entries
+        const int64_t max_listed = std::min<int64_t>(nv, vv.entries / (kMaxDeg + 1) + 1);
+        int32_t *list, *n_list, *scratch;
+        TRY(tmp.alloc(&list, max_listed));
+        TRY(tmp.alloc(&n_list, 1, true));
+        TRY(tmp.alloc(&scratch, vv.entries));
+        launch_crit_heavy(vv.off, vv.ent, v0, nv, max_listed, f, field_type, out, list, n_list,
+                          scratch, s);
+    }
     CK(cudaGetLastError());
     if (!out_on_device) {
         CK(cudaMemcpyAsync(classes_out, out, (size_t)nv * 12, cudaMemcpyDeviceToHost, s));
@@ -754,6 +811,8 @@ tg_status tg_mesh_destroy(tg_mesh *m)
     if (m->vtp) cudaFreeAsync(m->vtp, s);
     if (m->st_win) cudaFreeAsync(m->st_win, s);
     if (m->st_win_b) cudaFreeAsync(m->st_win_b, s);
+    if (m->st_wbase) cudaFreeAsync(m->st_wbase, s);
+    if (m->st_wbase_b) cudaFreeAsync(m->st_wbase_b, s);
     if (m->seg_c) cudaFreeAsync(m->seg_c, s);
     if (m->seg_ef) cudaFreeAsync(m->seg_ef, s);
     if (m->cadj) cudaFreeAsync(m->cadj, s);
@@ -800,15 +859,16 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     // the per-vertex cell counts and the first-cell bitmap: one zeroed
     // allocation
     const int64_t nwk = (4 * T + 31) / 32;
-    int32_t *deg_t;
+    int32_t *deg_t, *heavy_cnt;
     uint32_t *vflag;
     {
         Carve c;
-        const size_t o_d = c.add<int32_t>(V), o_f = c.add<uint32_t>(nwk);
+        const size_t o_d = c.add<int32_t>(V), o_f = c.add<uint32_t>(nwk), o_h = c.add<int32_t>(2);
         char *z;
         TRY(tmp.alloc(&z, (int64_t)c.bytes, true));
         deg_t = (int32_t *)(z + o_d);
         vflag = (uint32_t *)(z + o_f);
+        heavy_cnt = (int32_t *)(z + o_h);
     }
     int4 *occ;
     TRY(tmp.alloc(&occ, T));
@@ -830,12 +890,12 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     TRY(tmp.alloc(&vrank, nwk + 1));
     TRY(tmp.alloc(&vkey, V));
     TRY(tmp.alloc(&dcount, V));
-    launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, m->tvs, vflag, vkey, s);
+    launch_vt_sort(vt_off, m->vt_win, vt, V, 4 * T, m->tvs, vflag, vkey, heavy_cnt, s);
     {
         ScanJob jf{vflag, vrank, nwk, SCAN_POPC_RANK, 0};
         scan_batch(&jf, 1, m->scan, m->st, s);
         TRY(dalloc(&m->vorder, V, s));
-        launch_vorder_place(vt_off, V, vkey, vrank, nwk, m->vorder, dcount, s);
+        launch_vorder_place(vt_off, V, vkey, vrank, nwk, heavy_cnt, m->vorder, dcount, s);
         TRY(dalloc(&m->pofs, V + 1, s));
         ScanJob jd{dcount, m->pofs, V, SCAN_COUNT_I32, 0};
         scan_batch(&jd, 1, m->scan, m->st, s);
@@ -843,12 +903,20 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
         launch_vtp_fill(m->vorder, m->pofs, V, vt_off, vt, m->vtp, s);
         TRY(dalloc(&m->st_win, window_count(4 * T, star_window()) + 1, s));
         TRY(dalloc(&m->st_win_b, window_count(4 * T, star_window_b()) + 1, s));
+        TRY(dalloc(&m->st_wbase, window_count(4 * T, star_window()) + 1, s));
+        TRY(dalloc(&m->st_wbase_b, window_count(4 * T, star_window_b()) + 1, s));
         launch_window_starts(m->pofs, V, 4 * T, star_window(), m->st_win, s, star_window_b(),
-                             m->st_win_b);
+                             m->st_win_b, m->st_wbase, m->st_wbase_b);
     }
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
-    TRY(sync_read(m, s, 0, nullptr, nullptr));
+    // vertices with light stars, heavy ones and the heavy stars' entries
+    const void *rd[3] = {&vrank[nwk].y, heavy_cnt, heavy_cnt + 1};
+    const bool w8[3] = {false, false, false};
+    TRY(sync_read(m, s, 3, rd, w8));
+    m->n_light = T ? m->sz_host[0] : 0;
+    m->n_heavy = T ? m->sz_host[1] : 0;
+    m->heavy_entries = T ? m->sz_host[2] : 0;
     return check_flags(m);
 }
 

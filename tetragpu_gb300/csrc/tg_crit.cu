@@ -88,14 +88,21 @@ __device__ __forceinline__ void adj_scan(const int *row, int d, int top,
     }
 }
 
+// Rows longer than kMaxDeg (vertices whose classes tg_heavy.cu computes) are
+// not staged and get no masks; with heavy = 1 an entry (v, u) of a light v
+// whose neighbour u is such a vertex is computed from v's side whichever end
+// is lower (u computes nothing); heavy = 2 reports them instead
+// (ST_HEAVY_DEG) for callers without the heavy path.  Light rows start
+// below kAdjWin in their window and end below kAdjCap, so they always fit.
 __global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
-           const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st)
+           const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st,
+           int heavy)
 {
     griddep_wait();
     __shared__ int nb[kAdjCap];
     __shared__ int prow[2 * kAdjCap];   // the row starting at rs at 2 rs, INT_MAX to 2 rs + 2 d
-    __shared__ int meta[kAdjCap];   // row start | row length << 16
+    __shared__ int meta[kAdjCap];   // row start | row length << 16; -1: no light row there
     __shared__ int vid[kAdjCap];
     __shared__ int own[kAdjCap];
     __shared__ int s_vlo, s_vhi, s_n, n_own;
@@ -107,10 +114,12 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
         s_n = (int)(vv_off[s_vhi] - s_base);
         n_own = 0;
     }
+    if (heavy)
+        for (int e = threadIdx.x; e < kAdjCap; e += blockDim.x) meta[e] = -1;
     __syncthreads();
-    const int n = s_n;
+    const int n = min(s_n, kAdjCap);
     const long long base = s_base;
-    if (n > kAdjCap) {  // a row longer than kMaxDeg lies in this window
+    if (heavy == 2 && s_n > kAdjCap) {  // a row longer than kMaxDeg lies in this window
         if (threadIdx.x == 0) {
             atomicOr(&st->flags, ST_HEAVY_DEG);
             atomicMin(&st->bad_vertex, s_vlo);
@@ -121,8 +130,11 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
         const int rs = (int)(vv_off[v] - base);
         const int d = (int)(vv_off[v + 1] - vv_off[v]);
         if (d > kMaxDeg) {
-            atomicOr(&st->flags, ST_HEAVY_DEG);
-            atomicMin(&st->bad_vertex, v);
+            if (heavy == 2) {
+                atomicOr(&st->flags, ST_HEAVY_DEG);
+                atomicMin(&st->bad_vertex, v);
+            }
+            continue;
         }
         for (int i = 0; i < d; i++) {
             meta[rs + i] = rs | (d << 16);
@@ -132,10 +144,17 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
     for (int e = threadIdx.x; e < n; e += blockDim.x) nb[e] = __ldg(vv + base + e);
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int m = meta[e], rs = m & 0xffff, d = m >> 16;
+        const int m = meta[e];
+        if (m < 0) continue;
+        const int rs = m & 0xffff, d = m >> 16;
         prow[rs + e] = nb[e];            // 2 rs + (e - rs)
         prow[rs + e + d] = INT_MAX;
-        if (d <= kMaxDeg && nb[e] > vid[e]) own[atomicAdd(&n_own, 1)] = e;
+        bool mine = nb[e] > vid[e];
+        if (!mine && heavy == 1) {       // a heavy lower end computes nothing
+            const int u = nb[e];
+            mine = __ldg(vv_off + u + 1) - __ldg(vv_off + u) > kMaxDeg;
+        }
+        if (mine) own[atomicAdd(&n_own, 1)] = e;
     }
     __syncthreads();
     const int no = n_own;
@@ -146,7 +165,7 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
         const int v = vid[e], u = nb[e];
         const int64_t ub = vv_off[u];
         const int un = (int)(vv_off[u + 1] - ub);
-        if (un > kMaxDeg) continue;  // u's own block reports it
+        if (un > kMaxDeg && heavy != 1) continue;  // reported by u's own block
         // entries of u's row at or past the array's end are not loaded
         const int lim = (int)min(n_vv - ub, (int64_t)INT_MAX);
         int pv = -1;
@@ -165,7 +184,8 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
                                              pv);
         }
         adj[base + e] = bv;
-        if (pv >= 0) adj[ub + pv] = bu;
+        // u's mask is u's to keep only when u's row is light (else it has none)
+        if (pv >= 0 && un <= kMaxDeg) adj[ub + pv] = bu;
     }
 }
 
@@ -191,8 +211,9 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
     unsigned *classes3 = classes3_v0 - 3 * v0;
     const int64_t b = vv_off[v];
     const int n = (int)(vv_off[v + 1] - b);
+    if (n > kMaxDeg) return;   // tg_heavy.cu classifies it
     unsigned lo = 0, up = 0;
-    if (n <= kMaxDeg) {
+    {
         const F fv = field[v];
         unsigned long long lower = 0ull;
         for (int k = 0; k < n; k++) {
@@ -234,12 +255,13 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 int crit_window() { return kAdjWin; }
 
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
-                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s)
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, int heavy,
+                     cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
     launch_pdl(k_crit_adj, (unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s,
-        vv_off, vv, n_vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st);
+        vv_off, vv, n_vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st, heavy);
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,

@@ -170,11 +170,13 @@ void launch_vt_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, const int
                     int32_t *vt, cudaStream_t s);
 void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStream_t s);
 // Windows of win_size entries over a CSR: win[w] = first row starting at or
-// after entry win_size * w (w = 0 .. window_count), win[window_count] = rows.
+// after entry win_size * w (w = 0 .. window_count), win[window_count] = rows;
+// wbase[w] (when given) = that row's first entry, off[win[w]] (below 2^31).
 int64_t window_count(int64_t n_entries, int win_size);
 void launch_window_starts(const int64_t *off, int64_t rows, int64_t n_entries, int win_size,
                           int32_t *win, cudaStream_t s, int win_size2 = 0,
-                          int32_t *win2 = nullptr);
+                          int32_t *win2 = nullptr, int32_t *wbase = nullptr,
+                          int32_t *wbase2 = nullptr);
 int star_window();    // the window size of star pass A over VT
 int star_window_b();  // the window size of star pass B
 // sort every VT row (tg_star.cu): window-staged, coalesced.  Also marks each
@@ -182,26 +184,28 @@ int star_window_b();  // the window size of star pass B
 // zeroed by the caller) and stores it in vkey[v]; rows with no cells are left
 // alone.
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
-                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, cudaStream_t s);
+                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, int32_t *heavy_cnt,
+                    cudaStream_t s);
 // Star processing order (vertices by first cell): vorder[pos] = vertex and
 // dcount[pos] = its row length, pos = rank of its key; vtp = VT rows in that
 // order, pofs = its offsets (rows with no cells last, length 0)
 void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
-                         const uint2 *vrank, int64_t nwk, int32_t *vorder, int32_t *dcount,
-                         cudaStream_t s);
+                         const uint2 *vrank, int64_t nwk, const int32_t *heavy_cnt, int32_t *vorder,
+                         int32_t *dcount, cudaStream_t s);
 void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
                      const int32_t *vt, int32_t *vtp, cudaStream_t s);
 
 struct StarA {
     const int64_t *pofs;       // VT offsets in star processing order (rows + 1)
     const int32_t *win;        // window table over pofs
+    const int32_t *wbase;      // first entry of each window
     const int32_t *vorder;     // vertex at each processing position
     const int32_t *vtp;        // VT rows in processing order
     const int4 *tvs;
     int64_t V;
     int64_t nvt;               // VT entries (4 * cells)
     int32_t *deg;              // [V] neighbour counts (zeroed by the caller)
-    uint16_t *ecnt;            // [6T] ET | EF << 8 row lengths at owned edges' first slots
+    uint32_t *ecnt;            // [6T] ET | EF << 16 row lengths at owned edges' first slots
     uint32_t *eflag;           // bit per edge occurrence 6c+j (first occurrences)
     uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
     uint32_t *fbnd;            // bit per face occurrence: first and only (boundary face)
@@ -219,10 +223,10 @@ void launch_seg_ranks(const int64_t *seg_c, int64_t n, const uint2 *erank, const
 // len: E scratch words); edge_offsets_words = the tile words it needs in the
 // scan workspace
 int64_t edge_offsets_words(int64_t n_slots);
-void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
+void launch_edge_offsets(const uint32_t *eflag, const uint32_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
-                         uint32_t *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
+                         uint2 *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
 // FV, FT[f][0] and FF offsets in face-id order (nw = words of the face bitmap)
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
                        const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,
@@ -231,6 +235,7 @@ void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *b
 struct StarB {
     const int64_t *pofs;       // as in StarA
     const int32_t *win;        // window table over pofs with star_window_b()
+    const int32_t *wbase;      // first entry of each window
     const int32_t *vorder;
     const int32_t *vtp;
     const int4 *tvs;
@@ -268,11 +273,49 @@ void launch_tt_vertex_count(const int4 *tvs, int64_t T, const int64_t *vt_off, c
 void launch_tt_vertex_fill(const int4 *tvs, int64_t T, const int64_t *vt_off, const int32_t *vt,
                            const int64_t *tt_off, int32_t *tt, cudaStream_t s);
 
+// ---- heavy vertices (tg_heavy.cu) ----
+// Stars of more than kMaxStar cells: they follow every other vertex with
+// cells in the star processing order (positions n_light .. n_light +
+// n_heavy - 1), and these kernels do their share of star passes A and B.
+struct HeavyStars {
+    int64_t n_light, n_heavy;
+    const int64_t *pofs;
+    const int32_t *vorder;
+    const int32_t *vtp;
+    const int4 *tvs;
+    int2 *pairs;               // 3 per heavy star entry: (neighbour, position), sorted by pass A
+    int32_t *ids;              // 6 per heavy star entry (pass B scratch)
+    DevStatus *st;
+    // pass A
+    int32_t *deg;
+    uint32_t *ecnt, *eflag, *fflag, *fbnd;
+    // pass B
+    const int64_t *vv_off;
+    const uint2 *erank, *frank;
+    int32_t *vv, *eid_sorted, *te, *tf, *ft, *et, *ef;
+    const int64_t *et_off, *ef_off;
+};
+void launch_heavy_a(const HeavyStars &h, cudaStream_t s);
+void launch_heavy_b(const HeavyStars &h, cudaStream_t s);
+// EE rows of edges with an endpoint of more than kMaxDeg neighbours
+void launch_ee_heavy(const int32_t *ev, int64_t E, const int64_t *vv_off, const int32_t *eid,
+                     const int64_t *ee_off, int32_t *ee, cudaStream_t s);
+// classes of the vertices in [v0, v0 + nv) with more than kMaxDeg neighbours
+// (at most max_listed of them): list (capacity max_listed) and n_list (one
+// int, zeroed by the caller) are scratch, scratch holds one int per VV entry
+void launch_crit_heavy(const int64_t *vv_off, const int32_t *vv, int64_t v0, int64_t nv,
+                       int64_t max_listed, const void *field, int field_type, uint32_t *classes3,
+                       int32_t *list, int32_t *n_list, int32_t *scratch, cudaStream_t s);
+
 // critical points (tg_crit.cu)
 // vv_win: window table of VV (launch_window_starts over vv_off, crit_window())
 int crit_window();
+// heavy: 0 no row longer than kMaxDeg, 1 such rows get the heavy path
+// (masks of their light neighbours computed from the light side), 2 report
+// them with ST_HEAVY_DEG
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
-                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, cudaStream_t s);
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, int heavy,
+                     cudaStream_t s);
 // classify rows [v0, v0 + nv): field and classes3 hold nv values / rows from v0
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
                           const void *field, int field_type, int64_t v0, int64_t nv,

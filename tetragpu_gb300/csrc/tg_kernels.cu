@@ -412,7 +412,8 @@ k_ee_fill(const int *__restrict__ ev, int64_t E, const int64_t *__restrict__ vv_
         my_out = __ldg(ee_off + e0 + lane);
     }
     const unsigned small = __ballot_sync(kFull, lane < cnt && max(my_na, my_nb) <= 16);
-    const unsigned big = __ballot_sync(kFull, lane < cnt) & ~small;
+    // rows longer than kMaxDeg: the heavy path's (k_ee_heavy)
+    const unsigned big = __ballot_sync(kFull, lane < cnt && max(my_na, my_nb) <= kMaxDeg) & ~small;
     // small edges, 32 / G per round (group g takes the (k + g)-th one)
     constexpr int G = kEeGroup;
     const int g = lane / G, gl = lane % G;

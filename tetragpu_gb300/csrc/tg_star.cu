@@ -118,6 +118,7 @@ struct StageBaseA {
     int meta[kCap];                     // row start | D << 10 | slot of v << 20
     unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
     short cslot[kCap][3];               // hash slot of each entry's 3 candidates (other vertices)
+    unsigned head[kCap / 32 + 1];       // bit rs: a row starts at entry rs
     int n, vlo, vhi, full, wide;
     long long base;
 };
@@ -146,6 +147,7 @@ struct StageBaseB {
                                         // candidate): n_owned
                                         // owned ones (u > v) from the front, n_work others
                                         // from the back
+    unsigned head[kCapB / 32 + 1];      // bit rs: a row starts at entry rs
     int n, vlo, vhi, n_work, n_owned, wide;
     long long base;
 };
@@ -185,51 +187,74 @@ __device__ __forceinline__ unsigned long long hk(int rs, int u)
     return ((unsigned long long)(unsigned)rs << 32) | (unsigned)u;
 }
 
-// Stage the block's window: its bounds, every row's metadata (and whether a
-// star has more than kNarrowStar cells), empty hash keys.  Returns false
-// (block-uniformly) when the window cannot be handled here.  win[b] is the
-// first vertex whose row starts at or after entry kWin * b.
-__device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
-                           const int *__restrict__ win, const int *__restrict__ vorder,
-                           DevStatus *st)
+// Every entry's row: the row starts are marked in a bitmap (head), and an
+// entry's row start is the nearest mark at or below it (rows hold at most
+// kMaxStar entries, so the search looks at most three words back).  Only
+// the row starts' vid / meta are written by the rows; the other entries copy
+// theirs, all threads at once.
+__device__ __forceinline__ void fill_rows(const unsigned *head, int *vid, int *meta, int n)
 {
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        int w = e >> 5;
+        unsigned bits = head[w] & (0xffffffffu >> (31 - (e & 31)));
+        for (int k = 0; k < 3 && !bits && w > 0; k++) bits = head[--w];
+        const int rs = 32 * w + 31 - __clz(bits | 1u);
+        if (rs != e) {
+            vid[e] = vid[rs];
+            meta[e] = meta[rs];
+        }
+    }
+}
+
+// Stage the block's window: its bounds (the window table's entries, read by
+// every thread), every row's metadata (and whether a star has more than
+// kNarrowStar cells), empty hash keys.  Returns false (block-uniformly) when
+// the window cannot be handled here.  win[b] is the first vertex whose row
+// starts at or after entry kWin * b, wbase[b] that row's first entry.
+__device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
+                           const int *__restrict__ win, const int *__restrict__ wbase,
+                           const int *__restrict__ vorder, DevStatus *st)
+{
+    const int plo = __ldg(win + blockIdx.x), phi = __ldg(win + blockIdx.x + 1);
+    const int base = __ldg(wbase + blockIdx.x);
     if (threadIdx.x == 0) {
-        const int plo = win[blockIdx.x], phi = win[blockIdx.x + 1];
         S.vlo = plo;
         S.vhi = phi;
-        S.base = pofs[plo];
-        S.n = (int)(pofs[phi] - S.base);
+        S.base = base;
+        S.n = __ldg(wbase + blockIdx.x + 1) - base;
         S.full = 0;
         S.wide = 0;
     }
     for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hkey[h] = kEmpty;
+    for (int w = threadIdx.x; w < kCap / 32 + 1; w += blockDim.x) S.head[w] = 0u;
     __syncthreads();
-    if (S.n > kCap) {
-        if (threadIdx.x == 0) {
-            atomicOr(&st->flags, ST_HEAVY_STAR);
-            atomicMin(&st->bad_vertex, vorder[S.vlo]);
-        }
-        return false;
-    }
-    const long long base = S.base;
-    for (int i = S.vlo + threadIdx.x; i < S.vhi; i += blockDim.x) {
+    for (int i = plo + threadIdx.x; i < phi; i += blockDim.x) {
         const int rs = (int)(pofs[i] - base);
         const int D = (int)(pofs[i + 1] - pofs[i]);
         if (D == 0) continue;
-        const int v = vorder[i];
         if (D > kMaxStar) {
-            atomicOr(&st->flags, ST_HEAVY_STAR);
-            atomicMin(&st->bad_vertex, v);
-            S.full = 1;
+            // a heavy row: it and every row after it (heavy too) are
+            // tg_heavy.cu's; the window ends where it starts
+            atomicMin(&S.n, rs);
+            continue;
         }
         if (D > kNarrowStar) S.wide = 1;
-        for (int j = 0; j < D; j++) {
-            S.vid[rs + j] = v;
-            S.meta[rs + j] = rs | (D << 10);
-        }
+        S.vid[rs] = vorder[i];
+        S.meta[rs] = rs | (D << 10);
+        atomicOr(&S.head[rs >> 5], 1u << (rs & 31));
     }
     __syncthreads();
-    return !S.full;
+    const int n = S.n;
+    if (n > kCap) {   // cannot happen: light rows start below kWin and hold <= kMaxStar
+        if (threadIdx.x == 0) {
+            atomicOr(&st->flags, ST_HEAVY_STAR);
+            atomicMin(&st->bad_vertex, vorder[plo]);
+        }
+        return false;
+    }
+    fill_rows(S.head, S.vid, S.meta, n);
+    __syncthreads();
+    return true;
 }
 
 // Stage the window's cells and fill the (vertex, neighbour) table.  Returns
@@ -423,7 +448,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
         for (int off = 1; off < L; off <<= 1) n_ef += __shfl_xor_sync(0xffffffffu, n_ef, off);
         if (i < nw && sub == 0) {
             set_bit(a.eflag, p);
-            a.ecnt[p] = (unsigned short)(mpopc(mu) | (n_ef << 8));
+            a.ecnt[p] = (uint32_t)mpopc(mu) | ((uint32_t)n_ef << 16);
         }
     }
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -431,10 +456,10 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
         if (m_rs(m) != e) continue;
         const int d = cnt[e] & ~kRowBoundary;
         a.deg[S.vid[e]] = d;
-        if (d > kMaxDeg) {
-            atomicOr(&a.st->flags, ST_HEAVY_DEG);
-            atomicMax(&a.st->max_deg, d);
-        }
+        // vertices of more than kMaxDeg neighbours take the heavy paths of
+        // EE and critical points (tg_heavy.cu); the largest degree tells the
+        // host whether to launch them
+        if (d > kMaxDeg) atomicMax(&a.st->max_deg, d);
     }
 }
 
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
-    if (!stage_rows(S, a.pofs, a.win, a.vorder, a.st)) return;
+    if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.st)) return;
     if (S.wide)   // block-uniform
         star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, n_work);
     else
@@ -458,30 +483,35 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 // fails.
 __device__ void stage_rows_b(StageBaseB &S, const StarB &b)
 {
+    const int plo = __ldg(b.win + blockIdx.x), phi = __ldg(b.win + blockIdx.x + 1);
+    const int base = __ldg(b.wbase + blockIdx.x);
     if (threadIdx.x == 0) {
-        const int plo = b.win[blockIdx.x], phi = b.win[blockIdx.x + 1];
         S.vlo = plo;
         S.vhi = phi;
-        S.base = b.pofs[plo];
-        S.n = (int)(b.pofs[phi] - S.base);
+        S.base = base;
+        S.n = __ldg(b.wbase + blockIdx.x + 1) - base;
         S.n_work = 0;
         S.n_owned = 0;
         S.wide = 0;
     }
+    for (int w = threadIdx.x; w < kCapB / 32 + 1; w += blockDim.x) S.head[w] = 0u;
     __syncthreads();
-    const long long base = S.base;
-    for (int i = S.vlo + threadIdx.x; i < S.vhi; i += blockDim.x) {
+    for (int i = plo + threadIdx.x; i < phi; i += blockDim.x) {
         const int rs = (int)(b.pofs[i] - base);
         const int D = (int)(b.pofs[i + 1] - b.pofs[i]);
         if (D == 0) continue;
-        const int v = b.vorder[i];
-        if (D > kNarrowStar) S.wide = 1;
-        for (int j = 0; j < D; j++) {
-            S.vid[rs + j] = v;
-            S.meta[rs + j] = rs | (D << 10);
+        if (D > kMaxStar) {   // heavy rows (all after this one) are tg_heavy.cu's
+            atomicMin(&S.n, rs);
+            continue;
         }
+        if (D > kNarrowStar) S.wide = 1;
+        S.vid[rs] = b.vorder[i];
+        S.meta[rs] = rs | (D << 10);
         S.cnt[rs] = 0;
+        atomicOr(&S.head[rs >> 5], 1u << (rs & 31));
     }
+    __syncthreads();
+    fill_rows(S.head, S.vid, S.meta, S.n);
     __syncthreads();
 }
 
@@ -754,9 +784,19 @@ k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank
 // ---------------------------------------------------------------------------
 // Star processing order (see k_vorder_place): vertex v with first cell c in
 // slot k has key 4c + k; its bit in vflag marks it, its rank is v's position.
+// A vertex whose star holds more than kMaxStar cells is heavy: it takes no
+// key and is numbered among the heavy vertices instead (vkey = -1 - index),
+// which follow every other vertex with cells in the processing order, so
+// the star passes' windows never mix them with the rest (tg_heavy.cu
+// processes them).
 __device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_t *vflag,
-                                           int64_t *vkey, int v, int c)
+                                           int64_t *vkey, int *heavy_cnt, int v, int c, int64_t D)
 {
+    if (D > kMaxStar) {   // heavy_cnt[0]: heavy vertices, [1]: their star entries
+        vkey[v] = -1 - (long long)atomicAdd(heavy_cnt, 1);
+        atomicAdd(heavy_cnt + 1, (int)D);
+        return;
+    }
     const int4 w = __ldg(tvs + c);
     const long long key = 4LL * c + (w.x == v ? 0 : (w.y == v ? 1 : (w.z == v ? 2 : 3)));
     vkey[v] = key;
@@ -775,7 +815,8 @@ __device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_
 constexpr int kVtsThreads = TG_VTS_THREADS;
 __global__ void __launch_bounds__(kVtsThreads)
 k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt,
-          const int4 *__restrict__ tvs, uint32_t *__restrict__ vflag, int64_t *__restrict__ vkey)
+          const int4 *__restrict__ tvs, uint32_t *__restrict__ vflag, int64_t *__restrict__ vkey,
+          int *__restrict__ heavy_cnt)
 {
     griddep_wait();
     __shared__ int cell[kCap], out[kCap], meta[kCap];
@@ -803,7 +844,7 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
                 }
                 vt[j + 1] = x;
             }
-            if (e > b) mark_first(tvs, vflag, vkey, v, vt[b]);
+            if (e > b) mark_first(tvs, vflag, vkey, heavy_cnt, v, vt[b], e - b);
         }
         return;
     }
@@ -824,7 +865,8 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
     for (int e = threadIdx.x; e < n; e += blockDim.x) vt[base + e] = out[e];
     for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
         const int64_t b = vt_off[v];
-        if (vt_off[v + 1] > b) mark_first(tvs, vflag, vkey, v, out[b - base]);
+        if (vt_off[v + 1] > b)
+            mark_first(tvs, vflag, vkey, heavy_cnt, v, out[b - base], vt_off[v + 1] - b);
     }
 }
 
@@ -847,7 +889,7 @@ static_assert(kEdgeItems == 8 || kEdgeItems == 16 || kEdgeItems == 32, "slots pe
 
 struct EdgeOffsets {
     const uint32_t *eflag;
-    const unsigned short *ecnt;
+    const uint32_t *ecnt;
     const int4 *tvs;
     const int32_t *deg;
     const uint2 *erank;
@@ -856,7 +898,7 @@ struct EdgeOffsets {
     unsigned long long *next;    // the workspace buffer zeroed for the next user
     int64_t next_words;
     unsigned *err;
-    uint32_t *len;       // [E]: ET | EF << 8 | EE << 16
+    uint2 *len;          // [E]: {ET | EF << 16, EE}
     int64_t *et_off, *ef_off, *ee_off;
     int32_t *ev;         // [2E] or null: the edge's two vertices, ascending
     int64_t E;
@@ -953,13 +995,13 @@ __global__ void __launch_bounds__(kEdgeThreads, TG_EDGE_MINB) k_edge_offsets(Edg
         const int4 w = __ldg(p.tvs + cell);
         const int a = get4(w, j < 3 ? 0 : (j < 5 ? 1 : 2));
         const int b = get4(w, j < 3 ? j + 1 : (j == 3 ? 2 : 3));
-        const unsigned short c = p.ecnt[s];
-        const int et = c & 0xff, ef = c >> 8;
+        const uint32_t c = p.ecnt[s];
+        const int et = c & 0xffff, ef = c >> 16;
         const int ee = p.ee_off ? __ldg(p.deg + a) + __ldg(p.deg + b) - 2 : 0;
         x[0] += et;
         x[1] += ef;
         x[2] += ee;
-        p.len[id] = (uint32_t)c | ((uint32_t)ee << 16);
+        p.len[id] = make_uint2(c, (uint32_t)ee);
         if (p.ev) reinterpret_cast<int2 *>(p.ev)[id] = make_int2(a, b);
         id++;
     }
@@ -977,13 +1019,13 @@ __global__ void __launch_bounds__(kEdgeThreads, TG_EDGE_MINB) k_edge_offsets(Edg
     for (int q = 0; q < 3; q++) run[q] = s_pre[q] + excl[q];
     // this thread's packed words again (it wrote them: cache hits)
     for (int k = id0; k < id; k++) {
-        const uint32_t w = p.len[k];
+        const uint2 w = p.len[k];
         if (p.et_off) p.et_off[k] = run[0];
         if (p.ef_off) p.ef_off[k] = run[1];
         if (p.ee_off) p.ee_off[k] = run[2];
-        run[0] += w & 0xff;
-        run[1] += (w >> 8) & 0xff;
-        run[2] += w >> 16;
+        run[0] += w.x & 0xffff;
+        run[1] += w.x >> 16;
+        run[2] += w.y;
     }
     if (tile == p.n_tiles - 1 && threadIdx.x == 0) {
         if (p.et_off) p.et_off[p.E] = s_pre[0] + tot[0];
@@ -997,25 +1039,32 @@ __global__ void __launch_bounds__(kEdgeThreads, TG_EDGE_MINB) k_edge_offsets(Edg
 // off[v-1] < kWin * w <= off[v].  A second table over the same offsets with
 // another window size (win2, or null) comes from the same launch.
 __device__ __forceinline__ void window_owner(const long long lo, const long long hi, int64_t v,
-                                             int64_t n_win, int win_size, int *win)
+                                             int64_t n_win, int win_size, int *win, int *wbase,
+                                             long long base_v)
 {
     long long w = lo < 0 ? 0 : lo / win_size + 1;
     const long long w_hi = hi / win_size;
-    for (; w <= w_hi && w <= n_win; w++) win[w] = (int)v;
+    for (; w <= w_hi && w <= n_win; w++) {
+        win[w] = (int)v;
+        if (wbase) wbase[w] = (int)base_v;
+    }
 }
 
 __global__ void __launch_bounds__(256)
 k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int win_size,
-                int *__restrict__ win, int64_t n_win2, int win_size2, int *__restrict__ win2)
+                int *__restrict__ win, int64_t n_win2, int win_size2, int *__restrict__ win2,
+                int *__restrict__ wbase, int *__restrict__ wbase2)
 {
     griddep_wait();
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v > V) return;
     const long long lo = v == 0 ? -1 : off[v - 1];
-    window_owner(lo, v == V ? (long long)win_size * n_win : off[v], v, n_win, win_size, win);
+    const long long base_v = off[v];   // off[V] = the entry count
+    window_owner(lo, v == V ? (long long)win_size * n_win : off[v], v, n_win, win_size, win, wbase,
+                 base_v);
     if (win2)
         window_owner(lo, v == V ? (long long)win_size2 * n_win2 : off[v], v, n_win2, win_size2,
-                     win2);
+                     win2, wbase2, base_v);
 }
 
 // ---------------------------------------------------------------------------
@@ -1027,25 +1076,33 @@ k_window_starts(const int64_t *__restrict__ off, int64_t V, int64_t n_win, int w
 // cell gathers hit L2 and the output sectors of cell- and id-ordered
 // relations it writes are completed by blocks running at the same time.
 // k_vt_sort marks each vertex's key 4 * first cell + slot in a bitmap over
-// the 4T cell slots; the key's rank is the vertex's position.
+// the 4T cell slots; the key's rank is the vertex's position.  Heavy vertices
+// (vkey < 0) follow at n_light + their index; vertices without cells come
+// last.
 __global__ void __launch_bounds__(256)
 k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__restrict__ vkey,
-               const uint2 *__restrict__ vrank, int64_t nwk, int *__restrict__ vorder,
-               int *__restrict__ dcount)
+               const uint2 *__restrict__ vrank, int64_t nwk, const int *__restrict__ heavy_cnt,
+               int *__restrict__ vorder, int *__restrict__ dcount)
 {
     griddep_wait();
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
+    const int64_t n_light = (int64_t)__ldg(&vrank[nwk].y);
     // the positions past the vertices with cells (their rows are empty)
-    if (v >= (int64_t)__ldg(&vrank[nwk].y)) {
+    if (v >= n_light + *heavy_cnt) {
         vorder[v] = 0;
         dcount[v] = 0;
     }
     const int D = (int)(vt_off[v + 1] - vt_off[v]);
     if (D == 0) return;
     const long long key = vkey[v];
-    const uint2 r = __ldg(vrank + (key >> 5));
-    const int pos = (int)r.y + __popc(r.x & ((1u << (key & 31)) - 1u));
+    int64_t pos;
+    if (key < 0) {
+        pos = n_light + (-1 - key);
+    } else {
+        const uint2 r = __ldg(vrank + (key >> 5));
+        pos = (int64_t)r.y + __popc(r.x & ((1u << (key & 31)) - 1u));
+    }
     vorder[pos] = (int)v;
     dcount[pos] = D;
 }
@@ -1122,12 +1179,13 @@ int star_window_b() { return kWinB; }
 int64_t window_count(int64_t n_entries, int win_size) { return n_entries / win_size + 1; }
 
 void launch_window_starts(const int64_t *off, int64_t V, int64_t n_entries, int win_size,
-                          int32_t *win, cudaStream_t s, int win_size2, int32_t *win2)
+                          int32_t *win, cudaStream_t s, int win_size2, int32_t *win2,
+                          int32_t *wbase, int32_t *wbase2)
 {
     Launch L("k_window_starts", s);
     launch_pdl(k_window_starts, (unsigned)((V + 1 + 255) / 256), 256, 0, s,
         off, V, window_count(n_entries, win_size), win_size, win,
-        win2 ? window_count(n_entries, win_size2) : 0, win_size2, win2);
+        win2 ? window_count(n_entries, win_size2) : 0, win_size2, win2, wbase, wbase2);
 }
 
 int64_t edge_offsets_words(int64_t n_slots)
@@ -1135,15 +1193,15 @@ int64_t edge_offsets_words(int64_t n_slots)
     return 3 * ((n_slots + kEdgeTile - 1) / kEdgeTile) + 1;
 }
 
-void launch_edge_offsets(const uint32_t *eflag, const uint16_t *ecnt, const int4 *tvs,
+void launch_edge_offsets(const uint32_t *eflag, const uint32_t *ecnt, const int4 *tvs,
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
-                         uint32_t *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s)
+                         uint2 *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s)
 {
     const int64_t tiles = (n_slots + kEdgeTile - 1) / kEdgeTile;
     EdgeOffsets p{};
     p.eflag = eflag;
-    p.ecnt = reinterpret_cast<const unsigned short *>(ecnt);
+    p.ecnt = ecnt;
     p.tvs = tvs;
     p.deg = deg;
     p.erank = erank;
@@ -1189,22 +1247,24 @@ void launch_star_b(const StarB &b, cudaStream_t s)
 }
 
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
-                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, cudaStream_t s)
+                    int64_t nvt, const int4 *tvs, uint32_t *vflag, int64_t *vkey, int32_t *heavy_cnt,
+                    cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_vt_sort", s);
-    launch_pdl(k_vt_sort, n_windows(nvt), kVtsThreads, 0, s, vt_off, win, vt, tvs, vflag, vkey);
+    launch_pdl(k_vt_sort, n_windows(nvt), kVtsThreads, 0, s, vt_off, win, vt, tvs, vflag, vkey,
+               heavy_cnt);
 }
 
 
 void launch_vorder_place(const int64_t *vt_off, int64_t V, const int64_t *vkey,
-                         const uint2 *vrank, int64_t nwk, int32_t *vorder, int32_t *dcount,
-                         cudaStream_t s)
+                         const uint2 *vrank, int64_t nwk, const int32_t *heavy_cnt, int32_t *vorder,
+                         int32_t *dcount, cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_vorder_place", s);
     launch_pdl(k_vorder_place, (unsigned)((V + 255) / 256), 256, 0, s, vt_off, V, vkey, vrank, nwk,
-                                                                vorder, dcount);
+               heavy_cnt, vorder, dcount);
 }
 
 void launch_vtp_fill(const int32_t *vorder, const int64_t *pofs, int64_t V, const int64_t *vt_off,
