@@ -550,16 +550,19 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         m->F = F;
         if (m->seg_c) launch_seg_ranks(m->seg_c, m->n_seg, erank, frank, m->seg_ef, s);
         int64_t *et_off = nullptr, *ef_off = nullptr, *ee_off = nullptr;
-        if (mask & TG_ET) TRY(dalloc(&et_off, E + 1, s));
+        // EF rows are read off ET rows and TF (k_ef_fill): ET, TF and EV are
+        // made for EF too
+        const bool need_et = mask & (TG_ET | TG_EF);
+        if (need_et) TRY(dalloc(&et_off, E + 1, s));
         if (mask & TG_EF) TRY(dalloc(&ef_off, E + 1, s));
         if (mask & TG_EE) TRY(dalloc(&ee_off, E + 1, s));
         if (et_off) tmp.track(et_off);
         if (ef_off) tmp.track(ef_off);
         if (ee_off) tmp.track(ee_off);
-        // ---- pass B: ids, VV, fixed-width relations, ET and EF rows ----
-        const bool need_ev = mask & (TG_EV | TG_EE);
+        // ---- pass B: ids, VV, fixed-width relations, ET rows ----
+        const bool need_ev = mask & (TG_EV | TG_EE | TG_EF);
         const bool need_te = mask & (TG_TE | TG_FE);
-        const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF)) || want_tt_face;
+        const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF | TG_EF)) || want_tt_face;
         const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
         int32_t *vv, *eid_sorted = nullptr;
         int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
@@ -595,6 +598,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         const int64_t n_tt = 4 * T - n_bnd, n_ff = 3 * (2 * F - n_bnd);
         if (et_off) TRY(dalloc(&et, n_et, s));
         if (ef_off) TRY(dalloc(&ef, n_ef, s));
+        if (et && !(mask & TG_ET)) tmp.track(et);   // a temporary for EF (et_off is tracked)
         if (mask & TG_FE) TRY(dalloc(&fe, 3 * F, s));
         if (want_tt_face) {
             TRY(dalloc(&tt_off, T + 1, s));
@@ -612,7 +616,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
-        b.et_off = et_off; b.et = et; b.ef_off = ef_off; b.ef = ef; b.st = m->st;
+        b.et_off = et_off; b.et = et; b.st = m->st;
         side.join();
         launch_star_b(b, s);
         if (m->n_heavy > 0) {
@@ -625,9 +629,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             hv.tf = tf;
             hv.ft = ft;
             hv.et = et;
-            hv.ef = ef;
             hv.et_off = et_off;
-            hv.ef_off = ef_off;
             launch_heavy_b(hv, s);
         }
         tmp.keep(vv);
@@ -638,7 +640,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             m->cadj = nullptr;
         }
 
-        // the cell-ordered FE / TT and FF rows, and on request the link
+        // EF, the cell-ordered FE / TT and FF rows, and on request the link
         // adjacency of critical points, on a side stream beside EE (each
         // reads only what pass B and the passes before it wrote)
         const int64_t n_ee = sum_deg_sq - 2 * E;   // deg(a) + deg(b) - 2 per edge (a,b)
@@ -649,8 +651,9 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             TRY(dalloc(&m->cadj, nvv, s));
             TRY(tmp.alloc(&vv_win, window_count(nvv, crit_window()) + 1));
         }
-        if (fe || tt || ff_off || ff || prep_adj) {
+        if (fe || tt || ff_off || ff || ef || prep_adj) {
             const cudaStream_t s2 = side.fork();
+            if (ef) launch_ef_fill(ev, E, et_off, et, m->tvs, tf, ef_off, ef, s2);
             if (fe || tt || ff_off)
                 launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s2);
             if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
@@ -677,8 +680,9 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_FV) give_fixed(TG_REL_FV, fv, F);
         if (mask & TG_FT) give_fixed(TG_REL_FT, ft, F);
         if (fe) set_fixed(m, TG_REL_FE, fe, F);
-        if (et) {
+        if (et && (mask & TG_ET)) {
             tmp.keep(et_off);
+            tmp.keep(et);
             set_csr(m, TG_REL_ET, et_off, et, E, n_et);
         }
         if (ef) {

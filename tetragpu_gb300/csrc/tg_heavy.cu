@@ -265,8 +265,8 @@ __global__ void __launch_bounds__(64) k_heavy_a(HeavyStars h)
 
 // Pass B's share (the pairs stay sorted from pass A): VV row, edge ids and
 // the id-sorted incident edges, TE of the pairs v is the low end of, TF and
-// FT of the faces whose lowest vertex is v, ET and EF rows of the edges v
-// owns.
+// FT of the faces whose lowest vertex is v, ET rows of the edges v owns (EF
+// rows come from k_ef_fill, as for every edge).
 __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
 {
     griddep_wait();
@@ -294,29 +294,6 @@ __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
         if (u > v && h.et) {
             const int64_t o = h.et_off[id];
             for (int q = s0; q < s1; q++) h.et[o + (q - s0)] = s.cells[a[q].y];
-        }
-        if (u > v && h.ef) {
-            // faces (v, u, x) at their first cell, cells ascending, two faces
-            // of one cell by column (ascending first occurrence = face id)
-            int64_t o = h.ef_off[id];
-            for (int q = s0; q < s1; q++) {
-                const int c = s.cells[a[q].y];
-                const int4 w = h.tvs[c];
-                const int sj = slot_of(w, v), sk = slot_of(w, u);
-                int col[2], nf = 0;
-#pragma unroll
-                for (int t = 0; t < 4; t++) {
-                    if (t == sj || t == sk) continue;
-                    if (first_with(h, s.cells, a, s0, q, get4(w, t)))
-                        col[nf++] = 3 - (6 - sj - sk - t);   // the fourth slot is omitted
-                }
-                if (nf == 2 && col[0] > col[1]) {
-                    const int t2 = col[0];
-                    col[0] = col[1];
-                    col[1] = t2;
-                }
-                for (int f = 0; f < nf; f++) h.ef[o++] = rank_of(h.frank, 4LL * c + col[f]);
-            }
         }
         r++;
         s0 = s1;

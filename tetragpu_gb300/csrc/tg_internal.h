@@ -253,8 +253,6 @@ struct StarB {
     int32_t *ft;               // [2F] or null: writes FT[f][1]
     const int64_t *et_off;
     int32_t *et;               // or null
-    const int64_t *ef_off;
-    int32_t *ef;               // or null
     DevStatus *st;
 };
 void launch_star_b(const StarB &b, cudaStream_t s);
@@ -264,6 +262,10 @@ void launch_star_b(const StarB &b, cudaStream_t s);
 void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
                        const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fe,
                        int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
+// EF rows (one thread per edge) from ET, the sorted TV and TF
+void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const int32_t *et,
+                    const int4 *tvs, const int32_t *tf, const int64_t *ef_off, int32_t *ef,
+                    cudaStream_t s);
 void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64_t *ff_off,
                     int32_t *ff, cudaStream_t s);
 void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const int32_t *eid_sorted,
@@ -292,8 +294,8 @@ struct HeavyStars {
     // pass B
     const int64_t *vv_off;
     const uint2 *erank, *frank;
-    int32_t *vv, *eid_sorted, *te, *tf, *ft, *et, *ef;
-    const int64_t *et_off, *ef_off;
+    int32_t *vv, *eid_sorted, *te, *tf, *ft, *et;
+    const int64_t *et_off;
 };
 void launch_heavy_a(const HeavyStars &h, cudaStream_t s);
 void launch_heavy_b(const HeavyStars &h, cudaStream_t s);

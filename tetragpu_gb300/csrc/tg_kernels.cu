@@ -20,7 +20,8 @@
 //   k_sort_rows    sort each CSR row in place (VT, incident-edge rows)
 //   k_star_a/b/c   the per-vertex star passes (tg_star.cu)
 //   k_cell_fe_tt   FE (from TE of a face's first cell) and face-sharing TT
-//   k_ff_fill      FF;  k_ee_fill  EE;  k_tt_vertex_*  vertex-sharing TT
+//   k_ef_fill      EF from ET and TF;  k_ff_fill  FF;  k_ee_fill  EE;
+//   k_tt_vertex_*  vertex-sharing TT
 #include <algorithm>
 #include <climits>
 
@@ -242,6 +243,48 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__re
 #pragma unroll
         for (int i = 0; i < 4; i++)
             if (i < n) row[i] = nbr[i];
+    }
+}
+
+// EF rows, a thread per edge e = (a, b): walk its ET row (cells ascending)
+// and take at each cell the two faces holding a and b (the columns omitting
+// one of the other two slots), smaller id first, keeping an id only when it
+// exceeds the last one kept.  A face's id is the rank of its first
+// occurrence (4 * cell + column), so a face first met at this cell has a
+// larger id than every face met before, and a face met again (its second
+// cell) has an id no larger than the last kept: the row comes out ascending
+// with each face once.
+__global__ void __launch_bounds__(256)
+k_ef_fill(const int2 *__restrict__ ev, int64_t E, const int64_t *__restrict__ et_off,
+          const int *__restrict__ et, const int4 *__restrict__ tvs, const int *__restrict__ tf,
+          const int64_t *__restrict__ ef_off, int *__restrict__ ef)
+{
+    griddep_wait();
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const int2 ab = __ldg(ev + e);
+    const int64_t r0 = __ldg(et_off + e), r1 = __ldg(et_off + e + 1);
+    int *out = ef + __ldg(ef_off + e);
+    int last = -1, n = 0;
+    for (int64_t r = r0; r < r1; r++) {
+        const int c = __ldg(et + r);
+        const int4 w = __ldg(tvs + c);
+        // the slots of a and b (rows sorted, a < b), the other two t1 < t2
+        const int sa = (w.x < ab.x) + (w.y < ab.x) + (w.z < ab.x) + (w.w < ab.x);
+        const int sb = (w.x < ab.y) + (w.y < ab.y) + (w.z < ab.y) + (w.w < ab.y);
+        const int t1 = sa == 0 ? (sb == 1 ? 2 : 1) : 0;
+        const int t2 = 6 - sa - sb - t1;
+        // face omitting t: column 3 - t (t1 < t2: column 3 - t2 first)
+        const int f2 = __ldg(tf + 4LL * c + (3 - t2)), f1 = __ldg(tf + 4LL * c + (3 - t1));
+        const int lo = min(f1, f2), hi = max(f1, f2);
+        if (lo > last) {
+            out[n++] = lo;
+            last = lo;
+        }
+        if (hi > last) {
+            out[n++] = hi;
+            last = hi;
+        }
     }
 }
 
@@ -656,6 +699,16 @@ void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
         launch_pdl(k_cell_fe_tt, blocks_for(T, 256), 256, 0, s, tvs, T, F, te, tf, ft, brank, fe, tt_off,
                                                          tt, ff_off);
     }
+}
+
+void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const int32_t *et,
+                    const int4 *tvs, const int32_t *tf, const int64_t *ef_off, int32_t *ef,
+                    cudaStream_t s)
+{
+    if (E == 0) return;
+    Launch L("k_ef_fill", s);
+    launch_pdl(k_ef_fill, blocks_for(E, 256), 256, 0, s, reinterpret_cast<const int2 *>(ev), E,
+               et_off, et, tvs, tf, ef_off, ef);
 }
 
 void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64_t *ff_off,

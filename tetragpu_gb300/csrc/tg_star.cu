@@ -29,7 +29,7 @@
 //             ET / EF row lengths at each owned edge's first-occurrence slot,
 //             neighbour counts, the candidate masks
 //   k_star_b  ids (ranks of first occurrences), sorted VV rows, id-sorted
-//             incident edge ids, TE, TF, FT's second cell, ET and EF rows
+//             incident edge ids, TE, TF, FT's second cell, ET rows
 //   k_edge_offsets / k_face_slots  the id-ordered passes over occurrence
 //             slots: ET / EF / EE offsets and EV (one pass with a look-back
 //             scan); FV, FT's first cell, FF offsets
@@ -55,16 +55,10 @@ constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in th
 #define TG_STAR_WIN_B 224
 #endif
 constexpr int kWinB = TG_STAR_WIN_B;
-#ifndef TG_EF_LANES
-#define TG_EF_LANES 2
-#endif
-constexpr int kEfLanes = TG_EF_LANES;     // lanes per owned edge for its ET / EF rows (pass B)
 #ifndef TG_EFA_LANES
 #define TG_EFA_LANES 2
 #endif
 constexpr int kEfLanesA = TG_EFA_LANES;   // lanes per owned edge for its EF count (pass A)
-static_assert(kEfLanes == 1 || kEfLanes == 2 || kEfLanes == 4 || kEfLanes == 8,
-              "lanes per edge: 1, 2, 4 or 8");
 constexpr int kCapB = kWinB + kMaxStar;
 constexpr int kThreads = TG_STAR_THREADS;
 constexpr int kHashBits = TG_STAR_HASH_BITS;
@@ -600,85 +594,10 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
         __syncthreads();
     }
 
-    // 3a. the edges v owns, kEfLanes lanes to an edge, the lanes of an edge
-    //     taking its cells kEfLanes at a time in ascending order: ET rows
-    //     (cells of the star holding u, ascending) and EF rows (faces (v,u,x)
-    //     at their first cell, cells ascending, two faces of one cell by
-    //     column: ascending first occurrence, which is ascending face id); a
-    //     scan over the lanes places each cell's faces
-    if (b.et || b.ef) {
-        constexpr int L = kEfLanes;
-        const int span = ((n_owned * L + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x;
-        for (int t = threadIdx.x; t < span; t += blockDim.x) {   // block-uniform trip count
-            const int i = t / L, sub = t % L;
-            const bool act = i < n_owned;
-            int rs = 0, u = 0, id = 0;
-            M mu = 0;
-            if (act) {
-                const int e = (S.work[i] >> 2) & 511, k = S.work[i] & 3;
-                const int m = S.meta[e];
-                rs = m_rs(m);
-                u = get4(S.tv[e], k + (k >= m_sv(m)));
-                mu = S.cm[e][k];
-                id = S.hv[e][k];
-            }
-            const int rounds = (mpopc(mu) + L - 1) / L;
-            const int max_rounds = __reduce_max_sync(0xffffffffu, rounds);
-            long long et_p = act && b.et ? b.et_off[id] : 0;
-            long long ef_p = act && b.ef ? b.ef_off[id] : 0;
-            M rest = mu;
-            for (int r = 0; r < max_rounds; r++) {
-                // this lane's cell: the sub-th lowest remaining bit
-                M mine = rest;
-                for (int q = 0; q < sub; q++) mine &= mine - 1;
-                const int j = mine ? mctz(mine) : -1;
-                int nf = 0, col0 = 0, col1 = 0;
-                long long q0 = 0;
-                if (j >= 0) {
-                    const int ej = rs + j;
-                    if (b.et) b.et[et_p + sub] = S.cell[ej];
-                    const int4 wj = S.tv[ej];
-                    const int sj = m_sv(S.meta[ej]);
-                    const int su = slot_of(wj, u);
-                    const int ku = cand_of(su, sj);
-#pragma unroll
-                    for (int kk = 0; kk < 3; kk++) {
-                        if (kk == ku) continue;
-                        if (mctz(mu & S.cm[ej][kk]) != j) continue;
-                        const int tx = kk + (kk >= sj);
-                        const int c = 3 - (6 - sj - su - tx);   // the omitted slot is the fourth
-                        if (nf == 0) col0 = c; else col1 = c;
-                        nf++;
-                    }
-                    if (nf == 2 && col0 > col1) {
-                        const int t2 = col0;
-                        col0 = col1;
-                        col1 = t2;
-                    }
-                    q0 = 4LL * S.cell[ej];
-                }
-                int x = nf;
-#pragma unroll
-                for (int off = 1; off < L; off <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, x, off, L);
-                    if (sub >= off) x += y;
-                }
-                const int tot = __shfl_sync(0xffffffffu, x, L - 1, L);
-                if (b.ef && nf > 0) {
-                    const long long p = ef_p + (x - nf);
-                    b.ef[p] = rank_of(b.frank, q0 + col0);
-                    if (nf == 2) b.ef[p + 1] = rank_of(b.frank, q0 + col1);
-                }
-                et_p += L;
-                ef_p += tot;
-#pragma unroll
-                for (int q = 0; q < L; q++) rest &= rest - 1;
-            }
-        }
-    }
-
-    // 3b. one pass over two kinds of items:
-    //    [0, n)          an entry: TE of the pairs v is the low end of, TF /
+    // 3. one pass over two kinds of items:
+    //    [0, n)          an entry: TE of the pairs v is the low end of and the
+    //                    entry's cell in those edges' ET rows (its place: the
+    //                    star positions below it holding the other end), TF /
     //                    FT's second cell of the faces v owns
     //    then n_first    a first sighting: its place among v's incident edge
     //                    ids (for EE)
@@ -690,9 +609,14 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
             const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
             const int4 w = S.tv[e];
             const int c = S.cell[e];
-            if (b.te) {
-                for (int t = sv + 1; t < 4; t++)
-                    b.te[6LL * c + pair_slot(sv, t)] = hv_of(S, e, cand_of(t, sv), rs, get4(w, t));
+            if (b.te || b.et) {
+                const M below = ((M)1 << pos) - (M)1;
+                for (int t = sv + 1; t < 4; t++) {
+                    const int k = t - 1;   // cand_of(t, sv) for t > sv
+                    const int id = hv_of(S, e, k, rs, get4(w, t));
+                    if (b.te) b.te[6LL * c + pair_slot(sv, t)] = id;
+                    if (b.et) b.et[b.et_off[id] + mpopc(S.cm[e][k] & below)] = c;
+                }
             }
             if (sv <= 1 && (b.tf || b.ft)) {
                 // faces v owns, handled at their first cell: TF of both
