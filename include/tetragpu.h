@@ -112,6 +112,20 @@ const char *tg_last_error_string(void);
 tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts,
                          int tv_on_device, void *stream, tg_mesh **out);
 
+/* The reference's cells are vtkIdType (int64; TV_Data::cells,
+ * include/datatypes.h.in:63-101, as its VTK loader get_TV_from_VTK in
+ * src/vtk_load.cu:46-298 fills them).  tg_tv_narrow_i64 copies 4 * n_cells
+ * such ids into int32, slots in their order (tg_mesh_create sorts rows), and
+ * refuses what does not narrow: TG_ERR_INVALID_MESH for an id outside
+ * [0, n_points) (the message names the cell), TG_ERR_UNSUPPORTED for more
+ * than 2^31 - 1 points.  Host only; needs no GPU. */
+tg_status tg_tv_narrow_i64(const int64_t *cells, int64_t n_cells, int64_t n_points, int32_t *out);
+
+/* tg_mesh_create from the reference's int64 host TV (tg_tv_narrow_i64, then
+ * tg_mesh_create with tv_on_device = 0). */
+tg_status tg_mesh_create_i64(const int64_t *tv, int64_t n_cells, int64_t n_verts, void *stream,
+                             tg_mesh **out);
+
 /* Frees the mesh's device memory, ordered on the stream of its last call and
  * waiting for that stream: destroy a mesh before the stream it last used. */
 tg_status tg_mesh_destroy(tg_mesh *mesh);

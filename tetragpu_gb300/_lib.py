@@ -74,6 +74,8 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_mesh_device_bytes": (i64, [vp]),
         "tg_kernel_launch_count": (i64, []),
         "tg_tuning_info": (C.c_char_p, []),
+        "tg_tv_narrow_i64": (C.c_int, [vp, i64, i64, vp]),
+        "tg_mesh_create_i64": (C.c_int, [vp, i64, i64, vp, P(vp)]),
         "tg_profile_kernel": (C.c_int, [C.c_char_p]),
         "tg_profile_read": (C.c_int, [P(C.c_double), P(i64), C.c_int]),
         "tg_batch_create": (C.c_int, [vp, vp, vp, i64, C.c_int, vp, P(vp)]),

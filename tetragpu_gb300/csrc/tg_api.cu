@@ -950,6 +950,36 @@ tg_status tg_mesh_create(const int32_t *tv, int64_t n_cells, int64_t n_verts, in
     return TG_OK;
 }
 
+tg_status tg_tv_narrow_i64(const int64_t *cells, int64_t n_cells, int64_t n_points, int32_t *out)
+{
+    if (n_cells < 0 || n_points < 0 || (n_cells > 0 && (!cells || !out)))
+        return fail(TG_ERR_INVALID_ARGUMENT, "bad sizes or NULL pointer");
+    if (n_points > INT_MAX)
+        return fail(TG_ERR_UNSUPPORTED, "%lld points: ids must fit int32 (at most 2^31-1 points)",
+                    (long long)n_points);
+    for (int64_t i = 0; i < 4 * n_cells; i++) {
+        const int64_t x = cells[i];
+        if (x < 0 || x >= n_points)
+            return fail(TG_ERR_INVALID_MESH, "cell %lld has vertex id %lld, outside [0, %lld)",
+                        (long long)(i / 4), (long long)x, (long long)n_points);
+        out[i] = (int32_t)x;
+    }
+    return TG_OK;
+}
+
+tg_status tg_mesh_create_i64(const int64_t *tv, int64_t n_cells, int64_t n_verts, void *stream,
+                             tg_mesh **out)
+{
+    if (!out) return fail(TG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (n_cells < 0 || n_cells > kMaxCells)
+        return fail(n_cells < 0 ? TG_ERR_INVALID_ARGUMENT : TG_ERR_UNSUPPORTED,
+                    "bad cell count %lld", (long long)n_cells);
+    std::vector<int32_t> tv32((size_t)(4 * n_cells));
+    TRY(tg_tv_narrow_i64(tv, n_cells, n_verts, tv32.data()));
+    return tg_mesh_create(tv32.data(), n_cells, n_verts, 0, stream, out);
+}
+
 tg_status tg_extract(tg_mesh *m, uint32_t mask, uint32_t options, void *stream)
 {
     if (!m) return fail(TG_ERR_INVALID_ARGUMENT, "mesh is NULL");

@@ -10,6 +10,8 @@
 
 #include "tetragpu_compat.h"
 
+static_assert(sizeof(vtkIdType) == sizeof(int64_t), "vtkIdType is 64-bit");
+
 namespace {
 
 std::mutex g_mu;
@@ -36,25 +38,11 @@ tg_mesh *register_tv(const TV_Data &tv)
     if (g_mesh && g_cells == tv.cells && g_ncells == tv.nCells && g_npoints == tv.nPoints)
         return g_mesh;
     release_locked();
-    // the library's TV is int32: refuse what does not narrow instead of
-    // letting an id wrap (the reference's vtkIdType is 64-bit)
-    if (tv.nCells < 0 || tv.nPoints < 0 || tv.nPoints > INT32_MAX) {
-        fprintf(stderr, "tetragpu: mesh: %lld points, %lld cells: the point count must lie in "
-                        "[0, 2^31-1]\n", (long long)tv.nPoints, (long long)tv.nCells);
-        return nullptr;
-    }
-    std::vector<int32_t> tv32((size_t)(4 * tv.nCells));
-    for (size_t i = 0; i < tv32.size(); i++) {
-        const vtkIdType x = tv.cells[i];
-        if (x < 0 || x >= tv.nPoints) {
-            fprintf(stderr, "tetragpu: mesh: cell %lld has vertex id %lld, outside [0, %lld)\n",
-                    (long long)(i / 4), (long long)x, (long long)tv.nPoints);
-            return nullptr;
-        }
-        tv32[i] = (int32_t)x;
-    }
+    // the library's TV is int32: ids that do not narrow are refused (the
+    // reference's vtkIdType is 64-bit)
     tg_mesh *m = nullptr;
-    if (tg_mesh_create(tv32.data(), tv.nCells, tv.nPoints, 0, nullptr, &m) != TG_OK) {
+    if (tg_mesh_create_i64(reinterpret_cast<const int64_t *>(tv.cells), tv.nCells, tv.nPoints,
+                           nullptr, &m) != TG_OK) {
         report("mesh");
         return nullptr;
     }
