@@ -40,6 +40,8 @@
 
 #include <stdint.h>
 
+#include "tetragpu_device.h"   /* tg_device_mesh (plain C structs) */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -98,8 +100,9 @@ typedef struct tg_mesh tg_mesh;
 /* Library version string. */
 const char *tg_version(void);
 
-/* The tile parameters the kernels use (window sizes of the star passes and
- * of the link adjacency), as a JSON object. */
+/* The tile parameters this build's kernels use (star-pass windows, block
+ * sizes, lanes per edge; the values tetragpu_gb300/tune.py selects), as a
+ * JSON object. */
 const char *tg_tuning_info(void);
 
 /* Description of the last error on this thread ("" if none). */
@@ -226,6 +229,23 @@ tg_status tg_critical_points(tg_mesh *mesh, const void *field, int field_type,
  * counts_out (may be NULL): vertices per code 0..4.  Host only. */
 tg_status tg_export_classes(const uint32_t *classes, int64_t n_verts, const char *path,
                             int per_vertex_lines, int64_t *counts_out);
+
+/* ---- reading resident relations in place ----------------------------------
+ * tetragpu_device.h declares tg_device_mesh and inline accessors for device
+ * code; tg_get_device_mesh fills one with the mesh's resident relations
+ * (NULL where a relation was not extracted).  Serves the reference's aim of
+ * algorithm kernels reading relations where they lie
+ * (src/cuda_extraction.cu:16-22). */
+tg_status tg_get_device_mesh(const tg_mesh *mesh, tg_device_mesh *out);
+
+/* An algorithm kernel built that way (a downstream consumer of VV): Laplacian
+ * smoothing of a float32 vertex field on the device, each of `iterations`
+ * steps replacing f[v] by the mean of f[v] and its neighbours' values.  in,
+ * out and scratch (needed when iterations > 1) are device arrays of n_verts
+ * floats, in may not alias out or scratch; extracts VV if needed.
+ * Stream-ordered. */
+tg_status tg_smooth_field(tg_mesh *mesh, const float *in, float *out, int iterations,
+                          float *scratch, void *stream);
 
 /* Bytes of device memory the mesh currently holds. */
 int64_t tg_mesh_device_bytes(const tg_mesh *mesh);

@@ -43,18 +43,25 @@ def _stale(target: str, deps: list) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
+def build(verbose: bool = False, force: bool = False, defines: dict | None = None,
+          out_dir: str | None = None) -> str:
+    """Compile every csrc/*.cu and link libtetragpu.so.  defines: extra -D
+    NAME=value (the tuning sweep's candidates), built under out_dir (its own
+    objects and library) instead of the package."""
     nvcc = _nvcc()
-    os.makedirs(BUILD, exist_ok=True)
+    build_dir = os.path.join(out_dir, "obj") if out_dir else BUILD
+    lib = os.path.join(out_dir, "libtetragpu.so") if out_dir else LIB
+    dflags = [f"-D{k}={v}" for k, v in sorted((defines or {}).items())]
+    os.makedirs(build_dir, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(INCLUDE, "*.h"))
     objs = []
     jobs = []
     for src in sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, *NVFLAGS, "-c", src, "-o", obj])
+            jobs.append([nvcc, *ARCH, *NVFLAGS, *dflags, "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             results = list(ex.map(lambda cmd: subprocess.run(cmd, capture_output=True, text=True), jobs))
@@ -63,12 +70,12 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(r.stdout)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stderr)
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs]
+    if force or jobs or _stale(lib, objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", lib, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -76,6 +76,8 @@ def load(path: str | None = None) -> C.CDLL:
         "tg_tuning_info": (C.c_char_p, []),
         "tg_tv_narrow_i64": (C.c_int, [vp, i64, i64, vp]),
         "tg_mesh_create_i64": (C.c_int, [vp, i64, i64, vp, P(vp)]),
+        "tg_smooth_field": (C.c_int, [vp, vp, vp, C.c_int, vp, vp]),
+        "tg_get_device_mesh": (C.c_int, [vp, vp]),
         "tg_profile_kernel": (C.c_int, [C.c_char_p]),
         "tg_profile_read": (C.c_int, [P(C.c_double), P(i64), C.c_int]),
         "tg_batch_create": (C.c_int, [vp, vp, vp, i64, C.c_int, vp, P(vp)]),
@@ -232,6 +234,14 @@ class Mesh:
         check(self._lib.tg_critical_points(self._h, fptr, ftype, int(bool(on_device)),
                                            out.ctypes.data, 0, _stream(stream)))
         return out
+
+    def smooth_field(self, in_ptr: int, out_ptr: int, iterations: int = 1,
+                     scratch_ptr: int | None = None, stream=None):
+        """Laplacian smoothing over VV of a float32 device field
+        (tg_smooth_field): device pointers in, out and (iterations > 1)
+        scratch, n_verts floats each."""
+        check(self._lib.tg_smooth_field(self._h, in_ptr, out_ptr, iterations, scratch_ptr,
+                                        _stream(stream)))
 
     def device_bytes(self) -> int:
         return int(self._lib.tg_mesh_device_bytes(self._h))
@@ -486,11 +496,21 @@ def tuning_info() -> dict:
 
 
 def batch_tuning() -> dict:
-    """How the batched path is tuned: the batch runs as one disjoint-union
-    mesh, so every kernel launches once with the tiles below, whatever the
-    sizes of its members."""
-    d = tuning_info()
-    d["selection"] = "one setting for every batch (the union's windows do not depend on member sizes)"
+    """How the batched path is tuned: the tile parameters compiled in, and the
+    sweep that chose them (tetragpu_gb300/tuning.json, written by
+    python -m tetragpu_gb300.tune) when it exists."""
+    import json
+    d = {"compiled": tuning_info()}
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            rec = json.load(f)
+        d.update({"sweep": "tetragpu_gb300/tuning.json", "selected": rec.get("selected"),
+                  "selected_defines": rec.get("selected_defines"),
+                  "best_per_bucket": rec.get("best_per_bucket"),
+                  "selected_margin_pct": rec.get("selected_margin_pct")})
+    else:
+        d["sweep"] = None
     return d
 
 

@@ -785,10 +785,13 @@ const char *tg_tuning_info(void)
     static std::string info;
     static std::once_flag once;
     std::call_once(once, [] {
-        char buf[256];
+        char buf[512];
         snprintf(buf, sizeof buf,
-                 "{\"star_a_window\": %d, \"star_b_window\": %d, \"adjacency_window\": %d}",
-                 star_window(), star_window_b(), crit_window());
+                 "{\"TG_STAR_WIN\": %d, \"TG_STAR_WIN_B\": %d, \"TG_STAR_THREADS\": %d, "
+                 "\"TG_EFA_LANES\": %d, \"TG_VTS_THREADS\": %d, \"TG_EDGE_ITEMS\": %d, "
+                 "\"TG_ADJ_WIN\": %d, \"TG_ADJ_THREADS\": %d, \"TG_EE_GROUP\": %d}",
+                 TG_STAR_WIN, TG_STAR_WIN_B, TG_STAR_THREADS, TG_EFA_LANES, TG_VTS_THREADS,
+                 TG_EDGE_ITEMS, TG_ADJ_WIN, TG_ADJ_THREADS, TG_EE_GROUP);
         info = buf;
     });
     return info.c_str();

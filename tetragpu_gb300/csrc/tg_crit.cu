@@ -30,9 +30,6 @@ namespace {
 // (v, u)'s mask and bit i (w's place in u's row) in (u, v)'s, which sits at
 // v's place in u's row.  A block takes the vertices whose VV rows start in a
 // 256-entry window (win); the entries it owns (u > v) form a work list.
-#ifndef TG_ADJ_THREADS
-#define TG_ADJ_THREADS 128
-#endif
 constexpr int kAdjCap = kAdjWin + kMaxDeg;
 constexpr int kAdjThreads = TG_ADJ_THREADS;
 

@@ -7,6 +7,7 @@
 #include <utility>
 
 #include "tetragpu.h"
+#include "tg_tuning.h"
 
 namespace tg {
 
@@ -39,9 +40,6 @@ constexpr int kMaxDeg = 64;
 
 // VV entries per window of the link-adjacency kernel (tg_crit.cu): its
 // window table has n_vv / kAdjWin + 2 entries
-#ifndef TG_ADJ_WIN
-#define TG_ADJ_WIN 256
-#endif
 constexpr int kAdjWin = TG_ADJ_WIN;
 static_assert(kAdjWin >= 64 && kAdjWin <= 4096, "link-adjacency window size");
 

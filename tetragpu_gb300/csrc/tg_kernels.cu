@@ -382,9 +382,6 @@ __device__ __forceinline__ void ee_merge_one(const int *__restrict__ eid, int64_
 // to a lane (position gl + G r): the same bitonic merge over 32 positions,
 // the strides of G and more between registers, the smaller ones between the
 // group's lanes.
-#ifndef TG_EE_GROUP
-#define TG_EE_GROUP 4
-#endif
 constexpr int kEeGroup = TG_EE_GROUP;
 static_assert(kEeGroup == 4 || kEeGroup == 8, "lanes per edge: 4 or 8");
 

@@ -38,26 +38,11 @@
 namespace tg {
 namespace {
 
-#ifndef TG_STAR_WIN
-#define TG_STAR_WIN 256
-#endif
-#ifndef TG_STAR_THREADS
-#define TG_STAR_THREADS 256
-#endif
-#ifndef TG_STAR_HASH_BITS
-#define TG_STAR_HASH_BITS 10
-#endif
 constexpr int kWin = TG_STAR_WIN;         // VT entries per block window
 constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in the window)
 // pass B stages less per entry (no hash), so smaller windows let eight of its
 // blocks share an SM
-#ifndef TG_STAR_WIN_B
-#define TG_STAR_WIN_B 224
-#endif
 constexpr int kWinB = TG_STAR_WIN_B;
-#ifndef TG_EFA_LANES
-#define TG_EFA_LANES 2
-#endif
 constexpr int kEfLanesA = TG_EFA_LANES;   // lanes per owned edge for its EF count (pass A)
 constexpr int kCapB = kWinB + kMaxStar;
 constexpr int kThreads = TG_STAR_THREADS;
@@ -733,9 +718,6 @@ __device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_
 // insertion sort per row in global memory.  A block's time is mostly a chain
 // of dependent loads (window, offsets, cells, first cells): small blocks put
 // more chains in flight per SM.
-#ifndef TG_VTS_THREADS
-#define TG_VTS_THREADS 64
-#endif
 constexpr int kVtsThreads = TG_VTS_THREADS;
 __global__ void __launch_bounds__(kVtsThreads)
 k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *__restrict__ vt,
@@ -803,9 +785,6 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
 // its edges' row lengths (packed in one word by id) and EV, scans the three
 // sums with a look-back over the tiles before it, then writes the offsets of
 // its edges from the packed words it just wrote.
-#ifndef TG_EDGE_ITEMS
-#define TG_EDGE_ITEMS 8
-#endif
 constexpr int kEdgeThreads = 256;
 constexpr int kEdgeItems = TG_EDGE_ITEMS;             // slots per thread: 8, 16 or 32
 constexpr int kEdgeTile = kEdgeItems * kEdgeThreads;  // slots per tile
@@ -880,9 +859,6 @@ __device__ __forceinline__ uint32_t slot_bits(const EdgeOffsets &p, long long s0
 
 // eight blocks per SM (32 registers): the extra resident blocks hide the
 // gathers' latency better than the few spilled registers cost
-#ifndef TG_EDGE_MINB
-#define TG_EDGE_MINB 8
-#endif
 __global__ void __launch_bounds__(kEdgeThreads, TG_EDGE_MINB) k_edge_offsets(EdgeOffsets p)
 {
     griddep_wait();
@@ -1034,12 +1010,6 @@ k_vorder_place(const int64_t *__restrict__ vt_off, int64_t V, const int64_t *__r
 // VT rows copied into processing order: a warp fetches 32 rows' positions
 // and sources at once, then copies them one after another, lanes across the
 // row
-#ifndef TG_VTP_ROWS
-#define TG_VTP_ROWS 8
-#endif
-#ifndef TG_VTP_MINB
-#define TG_VTP_MINB 4
-#endif
 constexpr int kVtpRows = TG_VTP_ROWS;
 __global__ void __launch_bounds__(256, TG_VTP_MINB)
 k_vtp_fill(const int *__restrict__ vorder, const int64_t *__restrict__ pofs, int64_t V,
