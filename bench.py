@@ -228,15 +228,52 @@ def cpu_sample(mesh):
     return tv, mesh.n_verts, mesh.field
 
 
+# the 7 relations the reference's CPU code implements (TE, EV, ET, TF, FV,
+# VT, VV: make_TE_and_VE, make_TF_and_VF, elective_make_*)
+REF_BUILD_MASK = sum(1 << i for i in (1, 2, 3, 4, 5, 9, 13))
+
+
+def reference_build_baseline(mesh, workload: str) -> dict | None:
+    """The reference's own CPU code (src/cpu_extraction.cpp, compiled
+    unmodified into oracle/_ref/libtgref.so where the reference tree was
+    present at build time) on the same sample, for the 7 relations it
+    implements, beside the port on the same 7; None where that build does
+    not exist (the GPU host has no reference tree)."""
+    from oracle import oracle as O
+    if not O.Reference.available():
+        return None
+    O.build()
+    tv, nv, _ = cpu_sample(mesh)
+    orc, ref = O.Oracle(), O.Reference()
+    tvs = orc.canonicalize(tv, nv)
+    t_ref, t_port = [], []
+    for _ in range(2):
+        t_ref.append(ref.extract(tvs, nv)["seconds"])
+        t0 = time.perf_counter()
+        orc.extract(tvs, nv, mask=REF_BUILD_MASK)
+        t_port.append(time.perf_counter() - t0)
+    n = tv.shape[0]
+    return {"value": round(n / min(t_ref) / 1e6, 4), "unit": UNIT, "cores": 1,
+            "kind": "reference_build",
+            "relations": "TE EV ET TF FV VT VV (the 7 the reference implements on the CPU)",
+            "port_same_relations": round(n / min(t_port) / 1e6, 4),
+            "sample": f"cells [0, {n}) of the {workload} mesh, row-sorted, single thread, "
+                      f"best of 2 ({min(t_ref):.2f} s reference, {min(t_port):.2f} s port)"}
+
+
 def cpu_baseline(mesh, workload: str = WORKLOAD) -> dict:
     from oracle import oracle as O
     O.build()
     tv, nv, field = cpu_sample(mesh)
     times = _cpu_sample_worker((tv, nv, field, 2))
     t = min(times)
-    return {"value": round(tv.shape[0] / t / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"cells [0, {tv.shape[0]}) of the {workload} mesh, all 13 relations + "
-                      f"critical points, single thread, best of 2 ({t:.2f} s)"}
+    out = {"value": round(tv.shape[0] / t / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": f"cells [0, {tv.shape[0]}) of the {workload} mesh, all 13 relations + "
+                     f"critical points, single thread, best of 2 ({t:.2f} s)"}
+    rb = reference_build_baseline(mesh, workload)
+    out["reference_build"] = rb if rb else \
+        "not on this host: the reference's own CPU build needs the reference source tree"
+    return out
 
 
 def run_reference(args):
@@ -270,6 +307,9 @@ def run_reference(args):
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    rb = reference_build_baseline(mesh, workload)
+    if rb:
+        line["cpu_baseline"]["reference_build"] = rb
     print(json.dumps(line), flush=True)
 
 

@@ -45,7 +45,7 @@ class _RefResult(C.Structure):
                 ("et_off", C.POINTER(C.c_int64)), ("vt_off", C.POINTER(C.c_int64)),
                 ("vv_off", C.POINTER(C.c_int64)),
                 ("et", C.POINTER(C.c_int32)), ("vt", C.POINTER(C.c_int32)),
-                ("vv", C.POINTER(C.c_int32))]
+                ("vv", C.POINTER(C.c_int32)), ("seconds", C.c_double)]
 
 
 def build(force: bool = False) -> str:
@@ -182,6 +182,7 @@ class Reference:
             E, F = r.n_edges, r.n_faces
             out = {
                 "counts": (n_verts, E, F, T),
+                "seconds": r.seconds,
                 "TE": _copy(r.te, 6 * T, np.int32).reshape(T, 6),
                 "TF": _copy(r.tf, 4 * T, np.int32).reshape(T, 4),
                 "EV": _copy(r.ev, 2 * E, np.int32).reshape(E, 2),

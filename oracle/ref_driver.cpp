@@ -12,6 +12,7 @@
  * rest, and results are returned as flat arrays (VV in the reference's
  * first-encounter order; the comparison sorts rows).
  */
+#include <chrono>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -27,6 +28,7 @@ struct ref_result {
     int32_t *te, *tf, *ev, *fv;            /* fixed width */
     int64_t *et_off, *vt_off, *vv_off;     /* CSR, n_rows + 1 */
     int32_t *et, *vt, *vv;
+    double seconds;                        /* the reference functions alone (steady_clock) */
 };
 
 static int32_t *alloc_i32(size_t n) { return (int32_t *)malloc((n ? n : 1) * sizeof(int32_t)); }
@@ -62,6 +64,7 @@ int ref_extract(const int32_t *tvs, int64_t n_cells, int64_t n_verts, ref_result
     std::cout.rdbuf(sink.rdbuf());
     std::cerr.rdbuf(sink.rdbuf());
 
+    const auto t0 = std::chrono::steady_clock::now();
     TE_Data te(n_cells);
     VE_Data ve(n_verts);
     vtkIdType n_edges = make_TE_and_VE(tv, te, ve);
@@ -73,6 +76,7 @@ int ref_extract(const int32_t *tvs, int64_t n_cells, int64_t n_verts, ref_result
     std::unique_ptr<FV_Data> fv = elective_make_FV(vf, n_faces);
     std::unique_ptr<VV_Data> vv = elective_make_VV(tv, n_verts);
     std::unique_ptr<VT_Data> vt = elective_make_VT(tv);
+    out->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 
     std::cout.rdbuf(saved_out);
     std::cerr.rdbuf(saved_err);
