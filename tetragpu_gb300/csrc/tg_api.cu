@@ -452,6 +452,29 @@ void set_csr(tg_mesh *m, int r, int64_t *off, int32_t *ent, int64_t rows, int64_
     x.opts = opts;
 }
 
+// The link adjacency of critical points into m->cadj (allocated by the
+// caller), on stream s: VV's rows visited in the star processing order, so
+// that the neighbours' rows a window reads were read by the windows just
+// before it (in L2); the order's row lengths, their prefix and its window
+// table are temporaries of tmp.
+tg_status build_link_adjacency(tg_mesh *m, const int64_t *vv_off, const int32_t *vv, int64_t nvv,
+                               Temps &tmp, cudaStream_t s)
+{
+    const int64_t V = m->V;
+    int32_t *len, *win;
+    int64_t *ooff;
+    TRY(tmp.alloc(&len, V));
+    TRY(tmp.alloc(&ooff, V + 1));
+    TRY(tmp.alloc(&win, window_count(nvv, crit_window()) + 1));
+    launch_vv_lengths_in_order(vv_off, m->vorder, V, m->n_light + m->n_heavy, len, s);
+    ScanJob job{len, ooff, V, SCAN_COUNT_I32, 0};
+    scan_batch(&job, 1, m->scan, m->st, s);
+    launch_window_starts(ooff, V, nvv, crit_window(), win, s);
+    launch_crit_adj(vv_off, vv, m->vorder, ooff, win, V, nvv, m->cadj, m->st, m->max_deg ? 1 : 0,
+                    s);
+    return TG_OK;
+}
+
 tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
 {
     const int64_t V = m->V, T = m->T, NVT = 4 * T;
@@ -646,22 +669,14 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         const int64_t n_ee = sum_deg_sq - 2 * E;   // deg(a) + deg(b) - 2 per edge (a,b)
         if (ee_off) TRY(dalloc(&ee, n_ee, s));
         const bool prep_adj = (opts & TG_OPT_LINK_ADJACENCY) && (mask & TG_VV);
-        int32_t *vv_win = nullptr;
-        if (prep_adj) {
-            TRY(dalloc(&m->cadj, nvv, s));
-            TRY(tmp.alloc(&vv_win, window_count(nvv, crit_window()) + 1));
-        }
+        if (prep_adj) TRY(dalloc(&m->cadj, nvv, s));
         if (fe || tt || ff_off || ff || ef || prep_adj) {
             const cudaStream_t s2 = side.fork();
             if (ef) launch_ef_fill(ev, E, et_off, et, m->tvs, tf, ef_off, ef, s2);
             if (fe || tt || ff_off)
                 launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s2);
             if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
-            if (prep_adj) {
-                launch_window_starts(vv_off, V, nvv, crit_window(), vv_win, s2);
-                launch_crit_adj(vv_off, vv, vv_win, V, nvv, m->cadj, m->st, m->max_deg ? 1 : 0,
-                                s2);
-            }
+            if (prep_adj) TRY(build_link_adjacency(m, vv_off, vv, nvv, tmp, s2));
         }
         if (ee_off) {
             launch_ee_fill(ev, E, vv_off, eid_sorted, ee_off, ee, s);
@@ -736,14 +751,10 @@ tg_status tg::critical_points_rows(tg_mesh *m, int64_t v0, int64_t nv, const voi
     const Rel &vv = m->rel[TG_REL_VV];
     if (!m->cadj) {
         TRY(dalloc(&m->cadj, vv.entries, s));
-        int32_t *vv_win;
-        TRY(dalloc(&vv_win, window_count(vv.entries, crit_window()) + 1, s));
-        launch_window_starts(vv.off, V, vv.entries, crit_window(), vv_win, s);
-        // VV rows longer than the adjacency masks were already rejected by
-        // tg_extract (star pass A flags them), so no status read-back here
-        launch_crit_adj(vv.off, vv.ent, vv_win, V, vv.entries, m->cadj, m->st,
-                        m->max_deg ? 1 : 0, s);
-        cudaFreeAsync(vv_win, s);
+        // VV rows longer than the adjacency masks take the heavy path of the
+        // classification, so no status read-back here
+        Temps adj_tmp(s);
+        TRY(build_link_adjacency(m, vv.off, vv.ent, vv.entries, adj_tmp, s));
     }
     Temps tmp(s);
     const size_t esz = field_type == TG_FIELD_F64 ? 8 : 4;

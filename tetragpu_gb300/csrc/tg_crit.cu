@@ -91,8 +91,15 @@ __device__ __forceinline__ void adj_scan(const int *row, int d, int top,
 // is lower (u computes nothing); heavy = 2 reports them instead
 // (ST_HEAVY_DEG) for callers without the heavy path.  Light rows start
 // below kAdjWin in their window and end below kAdjCap, so they always fit.
+//
+// Windows run over the rows in `order` (the star processing order: vertices
+// by first cell, so consecutive windows share neighbours and the neighbours'
+// rows stay in L2; ooff = the row lengths' prefix in that order), or in id
+// order when order is null (ooff = vv_off).  A staged row keeps its global
+// start in gst[row start].
 __global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
+           const int *__restrict__ order, const int64_t *__restrict__ ooff,
            const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st,
            int heavy)
 {
@@ -102,13 +109,14 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
     __shared__ int meta[kAdjCap];   // row start | row length << 16; -1: no light row there
     __shared__ int vid[kAdjCap];
     __shared__ int own[kAdjCap];
+    __shared__ long long gst[kAdjCap];   // at a row start: the row's first entry in VV
     __shared__ int s_vlo, s_vhi, s_n, n_own;
     __shared__ long long s_base;
     if (threadIdx.x == 0) {
         s_vlo = win[blockIdx.x];
         s_vhi = win[blockIdx.x + 1];
-        s_base = vv_off[s_vlo];
-        s_n = (int)(vv_off[s_vhi] - s_base);
+        s_base = ooff[s_vlo];
+        s_n = (int)(ooff[s_vhi] - s_base);
         n_own = 0;
     }
     if (heavy)
@@ -119,13 +127,15 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
     if (heavy == 2 && s_n > kAdjCap) {  // a row longer than kMaxDeg lies in this window
         if (threadIdx.x == 0) {
             atomicOr(&st->flags, ST_HEAVY_DEG);
-            atomicMin(&st->bad_vertex, s_vlo);
+            atomicMin(&st->bad_vertex, order ? order[s_vlo] : s_vlo);
         }
         return;
     }
-    for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
-        const int rs = (int)(vv_off[v] - base);
-        const int d = (int)(vv_off[v + 1] - vv_off[v]);
+    for (int i = s_vlo + threadIdx.x; i < s_vhi; i += blockDim.x) {
+        const int rs = (int)(ooff[i] - base);
+        const int d = (int)(ooff[i + 1] - ooff[i]);
+        if (d == 0) continue;
+        const int v = order ? order[i] : i;
         if (d > kMaxDeg) {
             if (heavy == 2) {
                 atomicOr(&st->flags, ST_HEAVY_DEG);
@@ -133,12 +143,19 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
             }
             continue;
         }
-        for (int i = 0; i < d; i++) {
-            meta[rs + i] = rs | (d << 16);
-            vid[rs + i] = v;
+        gst[rs] = order ? vv_off[v] : base + rs;
+        for (int k = 0; k < d; k++) {
+            meta[rs + k] = rs | (d << 16);
+            vid[rs + k] = v;
         }
     }
-    for (int e = threadIdx.x; e < n; e += blockDim.x) nb[e] = __ldg(vv + base + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int m = meta[e];
+        if (heavy && m < 0) continue;
+        const int rs = m & 0xffff;
+        nb[e] = __ldg(vv + gst[rs] + (e - rs));
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = meta[e];
@@ -180,7 +197,7 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
                                              vec ? -(int)(ub & 3) : 0, un, lim, vec, v, bv, bu,
                                              pv);
         }
-        adj[base + e] = bv;
+        adj[gst[rs] + (e - rs)] = bv;
         // u's mask is u's to keep only when u's row is light (else it has none)
         if (pv >= 0 && un <= kMaxDeg) adj[ub + pv] = bu;
     }
@@ -251,14 +268,43 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 
 int crit_window() { return kAdjWin; }
 
-void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *vv_win,
-                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, int heavy,
-                     cudaStream_t s)
+void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *order,
+                     const int64_t *ooff, const int32_t *vv_win, int64_t V, int64_t n_vv,
+                     uint64_t *adj, DevStatus *st, int heavy, cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
     launch_pdl(k_crit_adj, (unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s,
-        vv_off, vv, n_vv, vv_win, reinterpret_cast<unsigned long long *>(adj), st, heavy);
+        vv_off, vv, n_vv, order, order ? ooff : vv_off, vv_win,
+        reinterpret_cast<unsigned long long *>(adj), st, heavy);
+}
+
+namespace {
+// row lengths of VV in the star processing order (positions past the
+// vertices with cells hold placeholders: length 0)
+__global__ void __launch_bounds__(256)
+k_vv_lengths_in_order(const int64_t *__restrict__ vv_off, const int *__restrict__ order,
+                      int64_t V, int64_t n_with_cells, int *__restrict__ len)
+{
+    griddep_wait();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    int d = 0;
+    if (i < n_with_cells) {
+        const int v = order[i];
+        d = (int)(vv_off[v + 1] - vv_off[v]);
+    }
+    len[i] = d;
+}
+}  // namespace
+
+void launch_vv_lengths_in_order(const int64_t *vv_off, const int32_t *order, int64_t V,
+                                int64_t n_with_cells, int32_t *len, cudaStream_t s)
+{
+    if (V == 0) return;
+    Launch L("k_vv_lengths_in_order", s);
+    launch_pdl(k_vv_lengths_in_order, (unsigned)((V + 255) / 256), 256, 0, s, vv_off, order, V,
+               n_with_cells, len);
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
