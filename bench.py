@@ -167,6 +167,24 @@ def output_bytes(counts: dict, totals: dict) -> int:
     return b
 
 
+def union_sizes(tg, batch) -> dict:
+    """Counts and CSR totals of a batch's union mesh (the sum over its
+    members), for output_bytes."""
+    C = tg._lib.C
+    lib = tg.load()
+    u = lib.tg_batch_union(batch._h)
+    v, e, f, t = (C.c_int64() for _ in range(4))
+    tg._lib.check(lib.tg_mesh_counts(u, C.byref(v), C.byref(e), C.byref(f), C.byref(t)))
+    totals = {}
+    for n in ("ET", "EF", "VT", "TT", "FF", "EE", "VV"):
+        off, ent = C.c_void_p(), C.c_void_p()
+        rows, cnt, width = C.c_int64(), C.c_int64(), C.c_int32()
+        tg._lib.check(lib.tg_get_relation(u, tg.REL[n], C.byref(off), C.byref(ent), C.byref(rows),
+                                          C.byref(cnt), C.byref(width)))
+        totals[n] = cnt.value
+    return {"counts_totals": ({"V": v.value, "E": e.value, "F": f.value, "T": t.value}, totals)}
+
+
 def kernel_bytes(name: str, c: dict, tot: dict) -> int:
     """Compulsory bytes one launch of a kernel is responsible for: the path's
     inputs it reads once and the final outputs it writes once.  Intermediates
@@ -340,10 +358,14 @@ def run_batch(args, torch, dist, tg, rank, local_rank, world, steps, e2e_steps):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
 
+    sizes = {}
+
     def batch_step():
         with tg.Batch(d_tv.data_ptr(), nv, n_cells=nc, on_device=True, stream=s) as b:
             b.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
             b.critical_points(d_f.data_ptr(), on_device=True, out_ptr=d_cls.data_ptr(), stream=s)
+            if not sizes:   # the union's counts and CSR totals: the batch's output bytes
+                sizes.update(union_sizes(tg, b))
 
     def loop_step():
         for i in range(len(meshes)):
@@ -383,6 +405,9 @@ def run_batch(args, torch, dist, tg, rank, local_rank, world, steps, e2e_steps):
     t_loop, loop_launches = timed(loop_step, steps)
     value = world * steps * T / t_batch / 1e6
     loop_value = world * steps * T / t_loop / 1e6
+    peak, peak_kind = peaks()
+    alg = output_bytes(*sizes["counts_totals"])
+    batch_gbs = alg / (t_batch / steps) / 1e9
 
     # e2e: host TV and fields in, every relation of the union and the classes
     # back to pinned host memory, through the batch API.  As for the single
@@ -470,6 +495,10 @@ def run_batch(args, torch, dist, tg, rank, local_rank, world, steps, e2e_steps):
                               "gpu_launches": int(loop_launches)},
             "batched_over_loop": round(value / loop_value, 3),
             "tuning": tg.batch_tuning(),
+            "roofline": {"bound": "hbm", "scope": "path (one batched step)",
+                         "achieved": round(batch_gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(batch_gbs / peak, 4), "peak_source": peak_kind,
+                         "algorithmic_bytes_per_step": alg, "traffic": None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
         }
@@ -479,14 +508,21 @@ def run_batch(args, torch, dist, tg, rank, local_rank, world, steps, e2e_steps):
 def main_batch(args, torch, dist, tg, rank, local_rank, world):
     line = run_batch(args, torch, dist, tg, rank, local_rank, world, args.steps, args.e2e_steps)
     if rank == 0:
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(load_workload("large")[1], WORKLOADS["large"])
         print(json.dumps(line), flush=True)
 
 
 def serve_requests(n_req: int, n_pool: int, seed: int):
-    """The request mix: a pool of seeded meshes (Kuhn grids, ids permuted, tet
-    counts lognormal with median 50k and sigma 1, capped at 4M) with four
-    Gaussian-mixture fields each; 70% of requests are new meshes drawn from the
-    pool, 30% new fields on a mesh an earlier request created."""
+    """The request mix, materialised before the stream starts.  Grids: a pool
+    of seeded Kuhn grids (the large mesh's generator: ids permuted), tet counts
+    lognormal with median 50k and sigma 1, capped at 4M, four Gaussian-mixture
+    fields each.  70% of requests are new meshes: a pool grid under a fresh
+    seeded vertex relabelling and slot shuffle, so that no two requests share a
+    mesh (ids, relations and classes all differ) while sizes follow the pool;
+    30% are new fields on the mesh of an earlier request (the field relabelled
+    the same way).  Returns the requests as ("mesh", tv, n_verts, field) or
+    ("field", index of the mesh request, field), and their tet counts."""
     from tetragpu_gb300 import meshgen
     rng = np.random.default_rng(seed)
     pool = []
@@ -497,29 +533,59 @@ def serve_requests(n_req: int, n_pool: int, seed: int):
         m.fields = [meshgen.gaussian_mixture_field(m.coords, n_gauss=8, seed=seed * 1000 + i * 7 + k,
                                                    noise=1e-3) for k in range(4)]
         pool.append(m)
-    reqs = []   # ("mesh", pool index, field index) or ("field", earlier request, field index)
+    reqs, tets, mesh_reqs = [], [], []
     for r in range(n_req):
-        meshes_so_far = [k for k, q in enumerate(reqs) if q[0] == "mesh"]
-        if meshes_so_far and rng.random() < 0.3:
-            reqs.append(("field", int(rng.choice(meshes_so_far)), int(rng.integers(0, 4))))
+        if mesh_reqs and rng.random() < 0.3:
+            k = int(rng.choice(mesh_reqs))
+            _, perm, pi = reqs[k][1:4]
+            m = pool[pi]
+            f = np.empty_like(m.fields[0])
+            f[perm] = m.fields[int(rng.integers(0, 4))]
+            reqs.append(("field", k, f))
+            tets.append(m.n_cells)
         else:
-            reqs.append(("mesh", int(rng.integers(0, n_pool)), int(rng.integers(0, 4))))
-    return pool, reqs
+            pi = int(rng.integers(0, n_pool))
+            m = pool[pi]
+            perm = rng.permutation(m.n_verts).astype(np.int32)
+            tv = rng.permuted(perm[m.tv], axis=1).astype(np.int32)
+            f = np.empty_like(m.fields[0])
+            f[perm] = m.fields[int(rng.integers(0, 4))]
+            reqs.append(("mesh", tv, perm, pi, m.n_verts, f))
+            tets.append(m.n_cells)
+            mesh_reqs.append(r)
+    return pool, reqs, tets
+
+
+def fifo_latencies(arrivals, service):
+    """Latencies of one server taking requests in arrival order, one at a
+    time: completion_i = max(completion_{i-1}, arrival_i) + service_i."""
+    done, out = 0.0, []
+    for t, sv in zip(arrivals, service):
+        done = max(done, t) + sv
+        out.append(done - t)
+    return out
 
 
 def main_serve(args, torch, tg, rank):
     """Serving: Poisson arrivals at swept rates into tg_server (continuous
     batching, 150 GB budget), against the plain per-request path (each request
-    alone through tg_mesh_*, resident meshes kept under the same budget)."""
+    alone through tg_mesh_*, resident meshes kept under the same budget).
+    Server latency = submission to result ready, measured (queueing
+    included).  Plain path: each request's service time measured back to
+    back, and its latency under the same arrivals computed as one server taking
+    requests in arrival order (queueing included, the same definition)."""
     n_req = args.serve_requests
-    pool, reqs = serve_requests(n_req, 64, 2468)
-    tets = [pool[q[1]].n_cells if q[0] == "mesh" else pool[reqs[q[1]][1]].n_cells for q in reqs]
+    t_gen = time.perf_counter()
+    pool, reqs, tets = serve_requests(n_req, 256, 2468)
+    t_gen = time.perf_counter() - t_gen
     total_tets = int(sum(tets))
     rates = [float(x) for x in args.serve_rates.split(",")]
     results = {}
+    arrivals = {}
     for rate in rates:
         rng = np.random.default_rng(int(rate))
         gaps = rng.exponential(1.0 / rate, size=n_req)
+        arrivals[rate] = np.cumsum(gaps)
         with tg.Server(n_slots=4, hbm_budget_bytes=150 * 10**9) as srv:
             rid, mid = [None] * n_req, [None] * n_req
             t0 = time.perf_counter()
@@ -529,11 +595,9 @@ def main_serve(args, torch, tg, rank):
                 while time.perf_counter() < t_next:
                     pass
                 if q[0] == "mesh":
-                    m = pool[q[1]]
-                    rid[k], mid[k] = srv.submit_mesh(m.tv, m.n_verts, m.fields[q[2]])
+                    rid[k], mid[k] = srv.submit_mesh(q[1], q[4], q[5])
                 else:
-                    m = pool[reqs[q[1]][1]]
-                    rid[k] = srv.submit_field(mid[q[1]], m.fields[q[2]])
+                    rid[k] = srv.submit_field(mid[q[1]], q[2])
             lat = []
             for k in range(n_req):
                 lat.append(srv.wait(rid[k])[1])
@@ -546,20 +610,19 @@ def main_serve(args, torch, tg, rank):
             "batches": st["batches"], "meshes_built": st["meshes_built"],
             "evictions": st["evictions"], "peak_gb": round(st["peak_bytes"] / 1e9, 2)}
 
-    # plain per-request path: one request at a time, back to back
+    # plain per-request path: one request at a time, back to back (service times)
     budget = 150 * 10**9
     resident, used, order = {}, 0, []
-    lat = []
+    service = []
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
     t0 = time.perf_counter()
     for k, q in enumerate(reqs):
         t1 = time.perf_counter()
         if q[0] == "mesh":
-            m = pool[q[1]]
-            g = tg.Mesh(m.tv, m.n_verts, stream=s)
+            g = tg.Mesh(q[1], q[4], stream=s)
             g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
-            g.critical_points(m.fields[q[2]], stream=s)
+            g.critical_points(q[5], stream=s)
             b = g.device_bytes()
             while order and used + b > budget:
                 old = order.pop(0)
@@ -570,23 +633,29 @@ def main_serve(args, torch, tg, rank):
             order.append(k)
             used += b
         else:
-            m = pool[reqs[q[1]][1]]
+            mq = reqs[q[1]]
             if resident.get(q[1]) is None:  # evicted: rebuild
-                g = tg.Mesh(m.tv, m.n_verts, stream=s)
+                g = tg.Mesh(mq[1], mq[4], stream=s)
                 g.extract(tg.ALL_RELATIONS, options=tg.OPT_LINK_ADJACENCY, stream=s)
                 resident[q[1]] = (g, g.device_bytes())
                 order.append(q[1])
                 used += resident[q[1]][1]
-            resident[q[1]][0].critical_points(m.fields[q[2]], stream=s)
-        lat.append((time.perf_counter() - t1) * 1e3)
+            resident[q[1]][0].critical_points(q[2], stream=s)
+        service.append(time.perf_counter() - t1)
     plain_wall = time.perf_counter() - t0
     for v in resident.values():
         if v is not None:
             v[0].close()
-    plain = {"p50_ms": round(float(np.percentile(lat, 50)), 3),
-             "p99_ms": round(float(np.percentile(lat, 99)), 3),
+    svc_ms = [x * 1e3 for x in service]
+    plain = {"service_p50_ms": round(float(np.percentile(svc_ms, 50)), 3),
+             "service_p99_ms": round(float(np.percentile(svc_ms, 99)), 3),
              "mtets_per_s": round(total_tets / plain_wall / 1e6, 3),
-             "wall_s": round(plain_wall, 3)}
+             "wall_s": round(plain_wall, 3), "under_arrivals": {}}
+    for rate in rates:
+        fl = [x * 1e3 for x in fifo_latencies(arrivals[rate], service)]
+        plain["under_arrivals"][str(int(rate))] = {
+            "p50_ms": round(float(np.percentile(fl, 50)), 3),
+            "p99_ms": round(float(np.percentile(fl, 99)), 3)}
     if rank == 0:
         top = results[str(int(rates[-1]))]
         line = {
@@ -594,12 +663,20 @@ def main_serve(args, torch, tg, rank):
             "steps": 1, "warmup": 0, "ms_per_step": round(top["wall_s"] * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic",
-            "config": {"workload": WORKLOADS["serve"], "requests": n_req, "mesh_pool": len(pool),
-                       "tets_requested": total_tets, "budget_gb": 150, "slots": 4,
-                       "timing": "wall clock, submission to completion per request"},
+            "config": {"workload": WORKLOADS["serve"], "requests": n_req,
+                       "mesh_requests": sum(1 for q in reqs if q[0] == "mesh"),
+                       "grid_pool": len(pool), "tets_requested": total_tets, "budget_gb": 150,
+                       "slots": 4, "generation_s": round(t_gen, 1),
+                       "meshes": "every mesh request a distinct mesh: a pool grid relabelled "
+                                 "and slot-shuffled with its own seed",
+                       "latency": "server: submission to result ready (queueing included); "
+                                  "plain: measured service times, latency under the same "
+                                  "arrivals as one server in arrival order"},
             "serving": results, "plain_per_request": plain,
             "p99_ms": top["p99_ms"], "p50_ms": top["p50_ms"],
         }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(load_workload("large")[1], WORKLOADS["large"])
         print(json.dumps(line), flush=True)
 
 
@@ -666,7 +743,7 @@ def main():
                 "ms_per_step": b["ms_per_step"], "steps": b["steps"],
                 "gpu_launches": b["gpu_launches"], "per_mesh_loop": b["per_mesh_loop"],
                 "batched_over_loop": b["batched_over_loop"], "tuning": b["tuning"],
-                "clocks": b["clocks"]}
+                "roofline": b["roofline"], "clocks": b["clocks"]}
             line["gpu_launches_batch_leg"] = b["gpu_launches"] + \
                 b["per_mesh_loop"]["gpu_launches"]
     if rank == 0:
