@@ -509,6 +509,15 @@ __device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b)
     __syncthreads();
 }
 
+// flat index (entry * 3 + candidate) of candidate u of entry e's first sighting
+template <typename M>
+__device__ __forceinline__ int first_slot(const StageM<M> &S, int e, int k, int rs, int u)
+{
+    const int f = rs + mctz(S.cm[e][k]);
+    if (f == e) return 3 * e + k;
+    return 3 * f + cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]));
+}
+
 // hv entry of candidate u of entry e: the one at u's first sighting in e's row
 template <typename M>
 __device__ __forceinline__ int hv_of(const StageM<M> &S, int e, int k, int rs, int u)
@@ -579,17 +588,38 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
         __syncthreads();
     }
 
-    // 3. one pass over two kinds of items:
-    //    [0, n)          an entry: TE of the pairs v is the low end of and the
-    //                    entry's cell in those edges' ET rows (its place: the
-    //                    star positions below it holding the other end), TF /
-    //                    FT's second cell of the faces v owns
-    //    then n_first    a first sighting: its place among v's incident edge
-    //                    ids (for EE)
-    const int n_items = n + (b.eid_sorted ? n_first : 0);
-    for (int i = threadIdx.x; i < n_items; i += blockDim.x) {
-        if (i < n) {
-            const int e = i;
+    // 3a. each first sighting's place among v's incident edge ids (for EE)
+    if (b.eid_sorted) {
+        for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
+            const int it = first_item(i);
+            const int e = (it >> 2) & 511, k = it & 3;
+            const int rs = m_rs(S.meta[e]);
+            const int id = S.hv[e][k];
+            const int deg = S.cnt[rs];
+            const int *li = S.list_u + 3 * rs;
+            int r = 0;
+            for (int j = 0; j < deg; j++) r += li[j] < id;
+            b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
+        }
+        __syncthreads();
+    }
+    // 3b. the ET offsets of the edges v owns, once per edge, at its first
+    //     sighting (in the neighbour lists' space, free from here on; ET
+    //     offsets are below 6T < 2^31)
+    int *eto = S.list_u;
+    if (b.et) {
+        for (int i = threadIdx.x; i < n_owned; i += blockDim.x) {
+            const int it = S.work[i];
+            const int e = (it >> 2) & 511, k = it & 3;
+            eto[3 * e + k] = (int)b.et_off[S.hv[e][k]];
+        }
+        __syncthreads();
+    }
+    // 3c. every entry: TE of the pairs v is the low end of and the entry's
+    //     cell in those edges' ET rows (its place: the star positions below
+    //     it holding the other end), TF / FT's second cell of the faces v owns
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        {
             const int m = S.meta[e];
             const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
             const int4 w = S.tv[e];
@@ -598,9 +628,10 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
                 const M below = ((M)1 << pos) - (M)1;
                 for (int t = sv + 1; t < 4; t++) {
                     const int k = t - 1;   // cand_of(t, sv) for t > sv
-                    const int id = hv_of(S, e, k, rs, get4(w, t));
+                    const int fs = first_slot(S, e, k, rs, get4(w, t));
+                    const int id = (&S.hv[0][0])[fs];
                     if (b.te) b.te[6LL * c + pair_slot(sv, t)] = id;
-                    if (b.et) b.et[b.et_off[id] + mpopc(S.cm[e][k] & below)] = c;
+                    if (b.et) b.et[(long long)eto[fs] + mpopc(S.cm[e][k] & below)] = c;
                 }
             }
             if (sv <= 1 && (b.tf || b.ft)) {
@@ -629,16 +660,6 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
                     }
                 }
             }
-        } else {
-            const int it = first_item(i - n);
-            const int e = (it >> 2) & 511, k = it & 3;
-            const int rs = m_rs(S.meta[e]);
-            const int id = S.hv[e][k];
-            const int deg = S.cnt[rs];
-            const int *li = S.list_u + 3 * rs;
-            int r = 0;
-            for (int j = 0; j < deg; j++) r += li[j] < id;
-            b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
         }
     }
 }
