@@ -5,6 +5,9 @@
 // candidates that way).
 #pragma once
 // BEGIN TUNED
+#ifndef TG_STAR_WIN_B
+#define TG_STAR_WIN_B 240
+#endif
 // END TUNED
 
 // defaults of the rest

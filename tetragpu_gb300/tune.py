@@ -41,6 +41,7 @@ TUNING_H = os.path.join(PKG, "csrc", "tg_tuning.h")
 CANDIDATES = [
     ("default", {}),
     ("star_b_win_192", {"TG_STAR_WIN_B": 192}),
+    ("star_b_win_240", {"TG_STAR_WIN_B": 240}),
     ("star_b_win_256", {"TG_STAR_WIN_B": 256}),
     ("star_a_win_192", {"TG_STAR_WIN": 192}),
     ("ee_group_8", {"TG_EE_GROUP": 8}),
