@@ -348,6 +348,7 @@ struct tg_mesh {
     // stars of more than kMaxStar cells (tg_heavy.cu): processing positions
     // n_light .. n_light + n_heavy - 1, heavy_entries VT entries in all
     int64_t n_light = 0, n_heavy = 0, heavy_entries = 0;
+    bool wide_stars = false;    // a light star holds more than 32 cells (64-bit star masks)
     int max_deg = 0;            // largest degree above kMaxDeg seen by the extraction, else 0
     uint64_t *cadj = nullptr;   // link adjacency for critical points, aligned with VV
     DevStatus *st = nullptr;    // device
@@ -520,10 +521,13 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         tmp.track(vv_off);  // owned by the VV relation once it is ready
         int64_t *deg_sq;  // prefix of deg^2: its total sizes EE (sum deg^2 - 2E)
         TRY(tmp.alloc(&deg_sq, V + 1));
-        uint64_t *emask;  // pass A's candidate masks, pass B's input
-        TRY(tmp.alloc(&emask, 3 * NVT));
+        // pass A's candidate masks, pass B's input: 32-bit unless a star
+        // holds more than 32 cells
+        const bool narrow = !m->wide_stars;
+        uint32_t *emask;
+        TRY(tmp.alloc(&emask, (narrow ? 3 : 6) * NVT));
         StarA a{m->pofs, m->st_win, m->st_wbase, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt,
-                eflag, fflag, fbnd, m->st, emask};
+                eflag, fflag, fbnd, m->st, emask, narrow};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));
@@ -637,7 +641,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.vtp = m->vtp;
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
-        b.emask = emask; b.vv = vv; b.eid_sorted = eid_sorted;
+        b.emask = emask; b.narrow = narrow; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.st = m->st;
         side.join();
@@ -881,7 +885,7 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     uint32_t *vflag;
     {
         Carve c;
-        const size_t o_d = c.add<int32_t>(V), o_f = c.add<uint32_t>(nwk), o_h = c.add<int32_t>(2);
+        const size_t o_d = c.add<int32_t>(V), o_f = c.add<uint32_t>(nwk), o_h = c.add<int32_t>(3);
         char *z;
         TRY(tmp.alloc(&z, (int64_t)c.bytes, true));
         deg_t = (int32_t *)(z + o_d);
@@ -928,13 +932,15 @@ static tg_status mesh_create_impl(const int32_t *tv, int64_t T, int64_t V, int o
     }
     CK(cudaGetLastError());
     set_csr(m, TG_REL_VT, vt_off, vt, V, 4 * T);
-    // vertices with light stars, heavy ones and the heavy stars' entries
-    const void *rd[3] = {&vrank[nwk].y, heavy_cnt, heavy_cnt + 1};
-    const bool w8[3] = {false, false, false};
-    TRY(sync_read(m, s, 3, rd, w8));
+    // vertices with light stars, heavy ones, the heavy stars' entries and
+    // whether a light star holds more than 32 cells
+    const void *rd[4] = {&vrank[nwk].y, heavy_cnt, heavy_cnt + 1, heavy_cnt + 2};
+    const bool w8[4] = {false, false, false, false};
+    TRY(sync_read(m, s, 4, rd, w8));
     m->n_light = T ? m->sz_host[0] : 0;
     m->n_heavy = T ? m->sz_host[1] : 0;
     m->heavy_entries = T ? m->sz_host[2] : 0;
+    m->wide_stars = T ? m->sz_host[3] != 0 : false;
     return check_flags(m);
 }
 

@@ -208,7 +208,8 @@ struct StarA {
     uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
     uint32_t *fbnd;            // bit per face occurrence: first and only (boundary face)
     DevStatus *st;
-    uint64_t *emask;           // [3][nvt] star positions holding each entry's candidates
+    void *emask;               // [3][nvt] star positions holding each entry's candidates
+    bool narrow;               // no star holds more than 32 cells: emask is 32-bit, else 64
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
 // seg_ef[i] = first edge id and seg_ef[n + 1 + i] = first face id of the
@@ -243,7 +244,8 @@ struct StarB {
     const uint2 *erank;        // {bits, prefix} per 32 edge occurrences
     const uint2 *frank;        // same for face occurrences
     const uint2 *brank;        // same for boundary-face occurrences
-    const uint64_t *emask;     // [3][nvt] from pass A
+    const void *emask;         // [3][nvt] from pass A
+    bool narrow;               // as in StarA
     int32_t *vv;               // [2E] VV rows
     int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null
     int32_t *te;               // [6T] or null

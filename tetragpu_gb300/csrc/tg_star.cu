@@ -326,8 +326,8 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 }
 
 // ---------------------------------------------------------------------------
-template <typename M>
-__device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_work)
+template <typename M, typename G>
+__device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emask, int &n_work)
 {
     // in the hash keys' space once the table is built (only its masks are
     // read after that): the first sightings of owned edges (entry << 2 |
@@ -350,7 +350,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             cm[k] = S.hmask[S.cslot[e][k]];
-            a.emask[k * a.nvt + S.base + e] = cm[k];
+            emask[k * a.nvt + S.base + e] = (G)cm[k];
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -442,6 +442,9 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_
     }
 }
 
+// G: the type the candidate masks are stored as (32-bit when no star of the
+// mesh holds more than kNarrowStar cells, so that no window is wide)
+template <typename G>
 __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 {
     griddep_wait();
@@ -449,10 +452,14 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
     if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.st)) return;
-    if (S.wide)   // block-uniform
-        star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, n_work);
-    else
-        star_a_body(*reinterpret_cast<Stage<unsigned> *>(raw), a, n_work);
+    G *emask = static_cast<G *>(a.emask);
+    if constexpr (sizeof(G) == 8) {
+        if (S.wide) {   // block-uniform
+            star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, emask, n_work);
+            return;
+        }
+    }
+    star_a_body(*reinterpret_cast<Stage<unsigned> *>(raw), a, emask, n_work);
 }
 
 // ---------------------------------------------------------------------------
@@ -494,8 +501,8 @@ __device__ void stage_rows_b(StageBaseB &S, const StarB &b)
     __syncthreads();
 }
 
-template <typename M>
-__device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b)
+template <typename M, typename G>
+__device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b, const G *emask)
 {
     const int n = S.n;
     const long long base = S.base;
@@ -504,7 +511,7 @@ __device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b)
         S.cell[e] = c;
         S.tv[e] = __ldg(b.tvs + c);
 #pragma unroll
-        for (int k = 0; k < 3; k++) S.cm[e][k] = (M)__ldg(b.emask + k * b.nvt + base + e);
+        for (int k = 0; k < 3; k++) S.cm[e][k] = (M)__ldg(emask + k * b.nvt + base + e);
     }
     __syncthreads();
 }
@@ -527,10 +534,10 @@ __device__ __forceinline__ int hv_of(const StageM<M> &S, int e, int k, int rs, i
     return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
 }
 
-template <typename M>
-__device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
+template <typename M, typename G>
+__device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b, const G *emask)
 {
-    stage_cells_b(S, b);
+    stage_cells_b(S, b, emask);
     const int n = S.n;
 
     // 1. list every vertex's neighbours (each at its first sighting); the
@@ -664,16 +671,21 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
     }
 }
 
+template <typename G>
 __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
 {
     griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(StageM<unsigned long long>)];
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
     stage_rows_b(S, b);
-    if (S.wide)   // block-uniform
-        star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b);
-    else
-        star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b);
+    const G *emask = static_cast<const G *>(b.emask);
+    if constexpr (sizeof(G) == 8) {
+        if (S.wide) {   // block-uniform
+            star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b, emask);
+            return;
+        }
+    }
+    star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask);
 }
 
 // The faces in id order, one thread per face occurrence q = 4 cell + col (a
@@ -727,6 +739,9 @@ __device__ __forceinline__ void mark_first(const int4 *__restrict__ tvs, uint32_
         atomicAdd(heavy_cnt + 1, (int)D);
         return;
     }
+    // heavy_cnt[2]: some light star holds more than kNarrowStar cells (the
+    // star passes then keep their candidate masks 64-bit in global memory)
+    if (D > kNarrowStar) heavy_cnt[2] = 1;
     const int4 w = __ldg(tvs + c);
     const long long key = 4LL * c + (w.x == v ? 0 : (w.y == v ? 1 : (w.z == v ? 2 : 3)));
     vkey[v] = key;
@@ -1141,7 +1156,10 @@ void launch_star_a(const StarA &a, cudaStream_t s)
 {
     if (a.V == 0) return;
     Launch L("k_star_a", s);
-    launch_pdl(k_star_a, n_windows(a.nvt), kThreads, 0, s, a);
+    if (a.narrow)
+        launch_pdl(k_star_a<uint32_t>, n_windows(a.nvt), kThreads, 0, s, a);
+    else
+        launch_pdl(k_star_a<uint64_t>, n_windows(a.nvt), kThreads, 0, s, a);
 }
 
 void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
@@ -1158,7 +1176,10 @@ void launch_star_b(const StarB &b, cudaStream_t s)
 {
     if (b.V == 0) return;
     Launch L("k_star_b", s);
-    launch_pdl(k_star_b, n_windows_b(b.nvt), kThreads, 0, s, b);
+    if (b.narrow)
+        launch_pdl(k_star_b<uint32_t>, n_windows_b(b.nvt), kThreads, 0, s, b);
+    else
+        launch_pdl(k_star_b<uint64_t>, n_windows_b(b.nvt), kThreads, 0, s, b);
 }
 
 void launch_vt_sort(const int64_t *vt_off, const int32_t *win, int32_t *vt, int64_t V,
