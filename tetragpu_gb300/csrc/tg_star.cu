@@ -86,6 +86,26 @@ __device__ __forceinline__ int mctz(unsigned long long m) { return __ffsll((long
 __device__ __forceinline__ int mpopc(unsigned m) { return __popc(m); }
 __device__ __forceinline__ int mpopc(unsigned long long m) { return __popcll(m); }
 constexpr int kNarrowStar = 32;   // the most cells a star may have for 32-bit masks
+
+// Asynchronous global -> shared copies (cp.async): the staging issues a
+// window's cell and vertex gathers this way before it loads the rows'
+// metadata, so the two chains of dependent loads overlap instead of running
+// one after the other, and no register holds the data in flight.  A thread
+// sees its own copies after cp_async_wait(); other threads' after that and
+// a barrier.
+template <int B>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem)
+{
+    static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (B == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(gmem), "n"(B)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 constexpr int kRowBoundary = 1 << 30;   // pass A's per-row count word: v has a boundary face
 
 // Pass A's shared memory: the fields that do not depend on the mask width
@@ -109,6 +129,7 @@ struct Stage : StageBaseA {
 // static shared memory is capped at 48 KiB per block
 static_assert(sizeof(Stage<unsigned long long>) <= 48 * 1024,
               "star stage exceeds the static shared-memory limit");
+static_assert(offsetof(StageBaseA, tv) % 16 == 0, "staged rows must be 16-byte aligned for cp.async");
 
 // Pass B stages the same window without a hash: pass A leaves every VT
 // entry's three candidate masks in global memory.  It also lists each
@@ -128,6 +149,7 @@ struct StageBaseB {
                                         // from the back
     unsigned head[kCapB / 32 + 1];      // bit rs: a row starts at entry rs
     int n, vlo, vhi, n_work, n_owned, wide;
+    int n_pairs, n_faces;               // the last phase's work lists
     long long base;
 };
 template <typename M>
@@ -136,6 +158,7 @@ struct StageM : StageBaseB {
 };
 static_assert(sizeof(StageM<unsigned long long>) <= 48 * 1024,
               "star stage B exceeds the static shared-memory limit");
+static_assert(offsetof(StageBaseB, tv) % 16 == 0, "staged rows must be 16-byte aligned for cp.async");
 
 __device__ __forceinline__ int m_rs(int m) { return m & 1023; }
 __device__ __forceinline__ int m_D(int m) { return (m >> 10) & 1023; }
@@ -186,16 +209,23 @@ __device__ __forceinline__ void fill_rows(const unsigned *head, int *vid, int *m
 }
 
 // Stage the block's window: its bounds (the window table's entries, read by
-// every thread), every row's metadata (and whether a star has more than
+// every thread), its cells and their sorted vertices (copied asynchronously,
+// issued first), every row's metadata (and whether a star has more than
 // kNarrowStar cells), empty hash keys.  Returns false (block-uniformly) when
 // the window cannot be handled here.  win[b] is the first vertex whose row
-// starts at or after entry kWin * b, wbase[b] that row's first entry.
+// starts at or after entry kWin * b, wbase[b] that row's first entry.  The
+// cells are staged up to the window's end before heavy rows clip it (at most
+// kCap entries, the most a window of light rows holds).
 __device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
                            const int *__restrict__ win, const int *__restrict__ wbase,
-                           const int *__restrict__ vorder, DevStatus *st)
+                           const int *__restrict__ vorder, const int *__restrict__ vtp,
+                           const int4 *__restrict__ tvs, DevStatus *st)
 {
     const int plo = __ldg(win + blockIdx.x), phi = __ldg(win + blockIdx.x + 1);
     const int base = __ldg(wbase + blockIdx.x);
+    const int nst = min(__ldg(wbase + blockIdx.x + 1) - base, kCap);
+    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<4>(&S.cell[e], vtp + base + e);
+    cp_async_commit();
     if (threadIdx.x == 0) {
         S.vlo = plo;
         S.vhi = phi;
@@ -222,6 +252,10 @@ __device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
         S.meta[rs] = rs | (D << 10);
         atomicOr(&S.head[rs >> 5], 1u << (rs & 31));
     }
+    // this thread's cells have landed: gather their vertices
+    cp_async_wait();
+    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<16>(&S.tv[e], tvs + S.cell[e]);
+    cp_async_commit();
     __syncthreads();
     const int n = S.n;
     if (n > kCap) {   // cannot happen: light rows start below kWin and hold <= kMaxStar
@@ -232,25 +266,18 @@ __device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
         return false;
     }
     fill_rows(S.head, S.vid, S.meta, n);
+    cp_async_wait();
     __syncthreads();
     return true;
 }
 
-// Stage the window's cells and fill the (vertex, neighbour) table.  Returns
+// Fill the (vertex, neighbour) table from the staged cells.  Returns
 // false (block-uniformly) when the table overflows.
 template <typename M>
-__device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vtp,
-                                     const int4 *__restrict__ tvs, const int *__restrict__ vorder,
-                                     DevStatus *st)
+__device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vorder, DevStatus *st)
 {
     for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hmask[h] = 0;
     const int n = S.n;
-    const long long base = S.base;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = __ldg(vtp + base + e);
-        S.cell[e] = c;
-        S.tv[e] = __ldg(tvs + c);
-    }
     __syncthreads();
     // insert the 3 other vertices of every staged cell, keyed by the row
     for (int e0 = 0; e0 < n; e0 += blockDim.x) {
@@ -335,7 +362,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
     static_assert(sizeof(S.hkey) >= 4 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
     int *cnt = work + 3 * kCap;
-    if (!stage_cells_and_hash(S, a.vtp, a.tvs, a.vorder, a.st)) return;
+    if (!stage_cells_and_hash(S, a.vorder, a.st)) return;
     const int n = S.n;
     for (int e = threadIdx.x; e < n; e += blockDim.x)
         if (m_rs(S.meta[e]) == e) cnt[e] = 0;
@@ -451,7 +478,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
-    if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.st)) return;
+    if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.vtp, a.tvs, a.st)) return;
     G *emask = static_cast<G *>(a.emask);
     if constexpr (sizeof(G) == 8) {
         if (S.wide) {   // block-uniform
@@ -463,14 +490,34 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 }
 
 // ---------------------------------------------------------------------------
-// Stage pass B's window: rows (and whether a star has more than kNarrowStar
-// cells), then cells, cell vertices and the candidate masks pass A computed.
-// Pass A has already rejected every window this cannot hold, so nothing here
-// fails.
-__device__ void stage_rows_b(StageBaseB &S, const StarB &b)
+// Stage pass B's window: cells (copied asynchronously, issued first), rows
+// (and whether a star has more than kNarrowStar cells), then the cells'
+// vertices and the candidate masks pass A computed, copied asynchronously
+// as soon as this thread's cells have landed.  Pass A has already rejected
+// every window this cannot hold, so nothing here fails.  Cells are staged up
+// to the window's end before heavy rows clip it (at most kCapB entries).
+// G: the masks' type in global memory; in shared memory they are 32-bit in
+// a window whose stars hold at most kNarrowStar cells (a narrow window of a
+// mesh with 64-bit masks copies their low halves), else 64-bit.
+template <typename M, typename G>
+__device__ __forceinline__ void copy_masks(StageM<M> &S, const StarB &b, const G *emask, int base,
+                                           int nst)
 {
+    for (int e = threadIdx.x; e < nst; e += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 3; k++)   // little-endian: the low half comes first
+            cp_async<sizeof(M)>(&S.cm[e][k], emask + k * b.nvt + base + e);
+}
+
+template <typename G>
+__device__ void stage_rows_b(unsigned char *raw, const StarB &b, const G *emask)
+{
+    StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
     const int plo = __ldg(b.win + blockIdx.x), phi = __ldg(b.win + blockIdx.x + 1);
     const int base = __ldg(b.wbase + blockIdx.x);
+    const int nst = min(__ldg(b.wbase + blockIdx.x + 1) - base, kCapB);
+    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<4>(&S.cell[e], b.vtp + base + e);
+    cp_async_commit();
     if (threadIdx.x == 0) {
         S.vlo = plo;
         S.vhi = phi;
@@ -478,6 +525,8 @@ __device__ void stage_rows_b(StageBaseB &S, const StarB &b)
         S.n = __ldg(b.wbase + blockIdx.x + 1) - base;
         S.n_work = 0;
         S.n_owned = 0;
+        S.n_pairs = 0;
+        S.n_faces = 0;
         S.wide = 0;
     }
     for (int w = threadIdx.x; w < kCapB / 32 + 1; w += blockDim.x) S.head[w] = 0u;
@@ -496,23 +545,23 @@ __device__ void stage_rows_b(StageBaseB &S, const StarB &b)
         S.cnt[rs] = 0;
         atomicOr(&S.head[rs >> 5], 1u << (rs & 31));
     }
+    cp_async_wait();
+    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<16>(&S.tv[e], b.tvs + S.cell[e]);
+    // with 32-bit masks in global memory every window is narrow; else the
+    // width is known once the rows are in
+    if constexpr (sizeof(G) == 4)
+        copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask, base, nst);
+    cp_async_commit();
     __syncthreads();
-    fill_rows(S.head, S.vid, S.meta, S.n);
-    __syncthreads();
-}
-
-template <typename M, typename G>
-__device__ __forceinline__ void stage_cells_b(StageM<M> &S, const StarB &b, const G *emask)
-{
-    const int n = S.n;
-    const long long base = S.base;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = __ldg(b.vtp + base + e);
-        S.cell[e] = c;
-        S.tv[e] = __ldg(b.tvs + c);
-#pragma unroll
-        for (int k = 0; k < 3; k++) S.cm[e][k] = (M)__ldg(emask + k * b.nvt + base + e);
+    if constexpr (sizeof(G) == 8) {
+        if (S.wide)
+            copy_masks(*reinterpret_cast<StageM<unsigned long long> *>(raw), b, emask, base, nst);
+        else
+            copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask, base, nst);
+        cp_async_commit();
     }
+    fill_rows(S.head, S.vid, S.meta, S.n);
+    cp_async_wait();
     __syncthreads();
 }
 
@@ -534,10 +583,9 @@ __device__ __forceinline__ int hv_of(const StageM<M> &S, int e, int k, int rs, i
     return S.hv[f][cand_of(slot_of(S.tv[f], u), m_sv(S.meta[f]))];
 }
 
-template <typename M, typename G>
-__device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b, const G *emask)
+template <typename M>
+__device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
 {
-    stage_cells_b(S, b, emask);
     const int n = S.n;
 
     // 1. list every vertex's neighbours (each at its first sighting); the
@@ -622,50 +670,84 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b, const 
         }
         __syncthreads();
     }
-    // 3c. every entry: TE of the pairs v is the low end of and the entry's
-    //     cell in those edges' ET rows (its place: the star positions below
-    //     it holding the other end), TF / FT's second cell of the faces v owns
+    // 3c. TE of the pairs v is the low end of and the entry's cell in those
+    //     edges' ET rows (its place: the star positions below it holding the
+    //     other end); TF / FT's second cell of the faces v owns, handled at
+    //     their first cell.  An entry holds 3 - sv such pairs and, at sv <= 1,
+    //     up to three faces, so a loop over entries would leave most lanes
+    //     idle; the pairs (entry << 2 | other slot) and the faces (entry << 2
+    //     | omitted slot) are listed first, in the spent first-sighting list
+    //     and row counts, and the lists run with every lane busy.  A window
+    //     with more first-cell faces than the face list holds handles its
+    //     faces entry by entry.
+    const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft;
+    int *pairs = S.work;   // <= 3 per entry
+    int *faces = S.cnt;    // <= kCapB, else the fallback below
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        {
+        const int m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        if (do_pairs && sv < 3) {
+            const int p0 = atomicAdd(&S.n_pairs, 3 - sv);
+            for (int t = sv + 1; t < 4; t++) pairs[p0 + t - sv - 1] = (e << 2) | t;
+        }
+        if (do_faces && sv <= 1) {
+            const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
+            for (int o = o_lo; o <= o_hi; o++) {
+                const int ko = cand_of(o, sv);
+                const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
+                if (mctz(S.cm[e][ka] & S.cm[e][kb]) != pos) continue;
+                const int q = atomicAdd(&S.n_faces, 1);
+                if (q < kCapB) faces[q] = (e << 2) | o;
+            }
+        }
+    }
+    __syncthreads();
+    const int n_pairs = S.n_pairs, n_faces = S.n_faces;
+    for (int i = threadIdx.x; i < n_pairs; i += blockDim.x) {
+        const int it = pairs[i];
+        const int e = it >> 2, t = it & 3, k = t - 1;   // cand_of(t, sv) for t > sv
+        const int m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
+        const int c = S.cell[e];
+        const int fs = first_slot(S, e, k, rs, get4(S.tv[e], t));
+        if (b.te) b.te[6LL * c + pair_slot(sv, t)] = (&S.hv[0][0])[fs];
+        if (b.et) b.et[(long long)eto[fs] + mpopc(S.cm[e][k] & (((M)1 << pos) - (M)1))] = c;
+    }
+    auto face = [&](int e, int o) {
+        const int m = S.meta[e];
+        const int rs = m_rs(m), sv = m_sv(m);
+        const int c = S.cell[e];
+        const int ko = cand_of(o, sv);
+        const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
+        const M mf = S.cm[e][ka] & S.cm[e][kb];
+        const int fid = rank_of(b.frank, 4LL * c + (3 - o));
+        if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
+        const M m2 = mf & (mf - 1);
+        if (!m2) {
+            if (b.ft) b.ft[2LL * fid + 1] = -1;
+            return;
+        }
+        const int j2 = rs + mctz(m2);
+        const int c2 = S.cell[j2];
+        if (b.ft) b.ft[2LL * fid + 1] = c2;
+        if (b.tf) {
+            int x, y;
+            face_others(S.tv[e], sv, o, x, y);
+            b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], S.vid[e], x, y))] = fid;
+        }
+    };
+    if (n_faces <= kCapB) {
+        for (int i = threadIdx.x; i < n_faces; i += blockDim.x) face(faces[i] >> 2, faces[i] & 3);
+    } else {
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
             const int m = S.meta[e];
             const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
-            const int4 w = S.tv[e];
-            const int c = S.cell[e];
-            if (b.te || b.et) {
-                const M below = ((M)1 << pos) - (M)1;
-                for (int t = sv + 1; t < 4; t++) {
-                    const int k = t - 1;   // cand_of(t, sv) for t > sv
-                    const int fs = first_slot(S, e, k, rs, get4(w, t));
-                    const int id = (&S.hv[0][0])[fs];
-                    if (b.te) b.te[6LL * c + pair_slot(sv, t)] = id;
-                    if (b.et) b.et[(long long)eto[fs] + mpopc(S.cm[e][k] & below)] = c;
-                }
-            }
-            if (sv <= 1 && (b.tf || b.ft)) {
-                // faces v owns, handled at their first cell: TF of both
-                // cells and FT's second cell, one face id load per face
-                const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
-                for (int o = o_lo; o <= o_hi; o++) {
-                    const int ko = cand_of(o, sv);
-                    const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
-                    const M mf = S.cm[e][ka] & S.cm[e][kb];
-                    if (mctz(mf) != pos) continue;
-                    const int fid = rank_of(b.frank, 4LL * c + (3 - o));
-                    if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
-                    const M m2 = mf & (mf - 1);
-                    if (!m2) {
-                        if (b.ft) b.ft[2LL * fid + 1] = -1;
-                        continue;
-                    }
-                    const int j2 = rs + mctz(m2);
-                    const int c2 = S.cell[j2];
-                    if (b.ft) b.ft[2LL * fid + 1] = c2;
-                    if (b.tf) {
-                        int x, y;
-                        face_others(w, sv, o, x, y);
-                        b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], S.vid[e], x, y))] = fid;
-                    }
-                }
+            if (sv > 1) continue;
+            const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
+            for (int o = o_lo; o <= o_hi; o++) {
+                const int ko = cand_of(o, sv);
+                const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
+                if (mctz(S.cm[e][ka] & S.cm[e][kb]) == pos) face(e, o);
             }
         }
     }
@@ -677,15 +759,14 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
     griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(StageM<unsigned long long>)];
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
-    stage_rows_b(S, b);
-    const G *emask = static_cast<const G *>(b.emask);
+    stage_rows_b(raw, b, static_cast<const G *>(b.emask));
     if constexpr (sizeof(G) == 8) {
         if (S.wide) {   // block-uniform
-            star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b, emask);
+            star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b);
             return;
         }
     }
-    star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask);
+    star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b);
 }
 
 // The faces in id order, one thread per face occurrence q = 4 cell + col (a
