@@ -597,14 +597,6 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         // each kernel goes out once its own buffers exist; the later
         // allocations are made while it runs
         if (need_ev) TRY(tmp.alloc(&ev, 2 * E));
-        // the id-ordered passes over the occurrence slots: the face slots on
-        // a side stream beside the edge offsets (a look-back scan that leaves
-        // issue slots free), joined before pass B
-        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
-        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
-        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
-        if (fv || ft || ff_off)
-            launch_face_slots(fflag, frank, brank, m->tvs, T, fv, ft, ff_off, side.fork());
         if (et_off || ef_off || ee_off || ev) {
             uint2 *len;
             TRY(tmp.alloc(&len, E));
@@ -616,6 +608,11 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
         if (need_te) TRY(tmp.alloc(&te, 6 * T));
         if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
+        // FV, FT and the FF offsets are written by pass B at each face's
+        // first cell
+        if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
+        if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
+        if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
         // CSR totals: ET = 6T, EF = 3F always; EE from the scan (read back
         // only when EE is wanted); TT and FF from the boundary-face count
         int32_t *et = nullptr, *ef = nullptr, *ee = nullptr, *ff = nullptr, *tt = nullptr,
@@ -642,9 +639,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.narrow = narrow; b.vv = vv; b.eid_sorted = eid_sorted;
-        b.te = te; b.tf = tf; b.ft = ft;
+        b.te = te; b.tf = tf; b.ft = ft; b.fv = fv; b.ff_off = ff_off;
         b.et_off = et_off; b.et = et; b.st = m->st;
-        side.join();
         launch_star_b(b, s);
         if (m->n_heavy > 0) {
             hv.vv_off = vv_off;
@@ -653,8 +649,11 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             hv.vv = vv;
             hv.eid_sorted = eid_sorted;
             hv.te = te;
+            hv.brank = brank;
             hv.tf = tf;
             hv.ft = ft;
+            hv.fv = fv;
+            hv.ff_off = ff_off;
             hv.et = et;
             hv.et_off = et_off;
             launch_heavy_b(hv, s);

@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
                 h.te[6LL * c + pair_slot(sv, t)] = id_at[lo];
             }
         }
-        if (sv > 1 || (!h.tf && !h.ft)) continue;
+        if (sv > 1 || (!h.tf && !h.ft && !h.fv && !h.ff_off)) continue;
         const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
         for (int o = o_lo; o <= o_hi; o++) {
             int x, y, x0, x1, y0, y1, f1, f2;
@@ -324,15 +324,10 @@ __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
             common_positions(a, x0, x1, y0, y1, f1, f2);
             if (f1 != j) continue;
             const long long q = 4LL * c + (3 - o);
-            const int fid = rank_of(h.frank, q);
-            if (h.tf) h.tf[q] = fid;
-            if (f2 < 0) {
-                if (h.ft) h.ft[2LL * fid + 1] = -1;
-                continue;
-            }
-            const int c2 = s.cells[f2];
-            if (h.ft) h.ft[2LL * fid + 1] = c2;
-            if (h.tf) h.tf[4LL * c2 + (3 - omitted_slot(h.tvs[c2], v, x, y))] = fid;
+            const int c2 = f2 < 0 ? -1 : s.cells[f2];
+            const int fid = face_at_first(h.frank, h.brank, h.tf, h.fv, h.ft, h.ff_off, q, c, c2,
+                                          v, x, y);
+            if (c2 >= 0 && h.tf) h.tf[4LL * c2 + (3 - omitted_slot(h.tvs[c2], v, x, y))] = fid;
         }
     }
 }

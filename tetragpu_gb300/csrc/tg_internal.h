@@ -226,10 +226,6 @@ void launch_edge_offsets(const uint32_t *eflag, const uint32_t *ecnt, const int4
                          const int32_t *deg, const uint2 *erank, int64_t n_slots, int64_t E,
                          int64_t *et_off, int64_t *ef_off, int64_t *ee_off, int32_t *ev,
                          uint2 *len, ScanWorkspace &ws, DevStatus *st, cudaStream_t s);
-// FV, FT[f][0] and FF offsets in face-id order (nw = words of the face bitmap)
-void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
-                       const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,
-                       cudaStream_t s);
 
 struct StarB {
     const int64_t *pofs;       // as in StarA
@@ -250,12 +246,42 @@ struct StarB {
     int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null
     int32_t *te;               // [6T] or null
     int32_t *tf;               // [4T] or null
-    int32_t *ft;               // [2F] or null: writes FT[f][1]
+    int32_t *ft;               // [2F] or null
+    int32_t *fv;               // [3F] or null
+    int64_t *ff_off;           // [F + 1] or null: FF offsets but the closing one
     const int64_t *et_off;
     int32_t *et;               // or null
     DevStatus *st;
 };
 void launch_star_b(const StarB &b, cudaStream_t s);
+
+// A face at its first cell c (occurrence q = 4c + TF column), owned by its
+// lowest vertex v, the others x < y, c2 its second cell or -1: its id is the
+// rank of q among first occurrences, and the face's FV row, FT row, FF
+// offset (3 * (2 * id - boundary faces before it)) and TF entry in c are
+// written here; the caller writes TF in c2.  Pass B and the heavy-star pass
+// call it, once per face.
+__device__ __forceinline__ int face_at_first(const uint2 *__restrict__ frank,
+                                             const uint2 *__restrict__ brank, int32_t *tf,
+                                             int32_t *fv, int32_t *ft, int64_t *ff_off,
+                                             long long q, int c, int c2, int v, int x, int y)
+{
+    const uint2 w = __ldg(frank + (q >> 5));
+    const unsigned below = (1u << (q & 31)) - 1u;
+    const int fid = (int)w.y + __popc(w.x & below);
+    if (tf) tf[q] = fid;
+    if (fv) {
+        fv[3LL * fid] = v;
+        fv[3LL * fid + 1] = x;
+        fv[3LL * fid + 2] = y;
+    }
+    if (ft) *reinterpret_cast<int2 *>(ft + 2LL * fid) = make_int2(c, c2);
+    if (ff_off) {
+        const uint2 bw = __ldg(brank + (q >> 5));
+        ff_off[fid] = 3LL * (2LL * fid - ((long long)bw.y + __popc(bw.x & below)));
+    }
+    return fid;
+}
 
 // FE of every face at its first cell; TT offsets (4c - boundary faces before
 // cell c), TT rows, and the closing FF offset.
@@ -293,8 +319,9 @@ struct HeavyStars {
     uint32_t *ecnt, *eflag, *fflag, *fbnd;
     // pass B
     const int64_t *vv_off;
-    const uint2 *erank, *frank;
-    int32_t *vv, *eid_sorted, *te, *tf, *ft, *et;
+    const uint2 *erank, *frank, *brank;
+    int32_t *vv, *eid_sorted, *te, *tf, *ft, *fv, *et;
+    int64_t *ff_off;
     const int64_t *et_off;
 };
 void launch_heavy_a(const HeavyStars &h, cudaStream_t s);
@@ -359,6 +386,24 @@ void prof_end(const char *name, cudaStream_t s);
 // signal their dependents early: blocks of the next kernel waiting on SMs
 // cost the running one more than the earlier start saves.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Asynchronous global -> shared copies (cp.async): no register holds the
+// data in flight, so a kernel can put many dependent-load chains' loads in
+// flight at once.  A thread sees its own copies after cp_async_wait(); other
+// threads' after that and a barrier.
+template <int B>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem)
+{
+    static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (B == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(gmem), "n"(B)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 template <typename... KArgs, typename... Args>
 inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                        Args &&...args)

@@ -29,10 +29,10 @@
 //             ET / EF row lengths at each owned edge's first-occurrence slot,
 //             neighbour counts, the candidate masks
 //   k_star_b  ids (ranks of first occurrences), sorted VV rows, id-sorted
-//             incident edge ids, TE, TF, FT's second cell, ET rows
-//   k_edge_offsets / k_face_slots  the id-ordered passes over occurrence
-//             slots: ET / EF / EE offsets and EV (one pass with a look-back
-//             scan); FV, FT's first cell, FF offsets
+//             incident edge ids, TE, TF, ET rows, and at each face's first
+//             cell its FV row, FT row and FF offset
+//   k_edge_offsets  the id-ordered pass over edge occurrence slots: ET / EF /
+//             EE offsets and EV (one pass with a look-back scan)
 #include "tg_internal.h"
 
 namespace tg {
@@ -87,25 +87,6 @@ __device__ __forceinline__ int mpopc(unsigned m) { return __popc(m); }
 __device__ __forceinline__ int mpopc(unsigned long long m) { return __popcll(m); }
 constexpr int kNarrowStar = 32;   // the most cells a star may have for 32-bit masks
 
-// Asynchronous global -> shared copies (cp.async): the staging issues a
-// window's cell and vertex gathers this way before it loads the rows'
-// metadata, so the two chains of dependent loads overlap instead of running
-// one after the other, and no register holds the data in flight.  A thread
-// sees its own copies after cp_async_wait(); other threads' after that and
-// a barrier.
-template <int B>
-__device__ __forceinline__ void cp_async(void *smem, const void *gmem)
-{
-    static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
-    if constexpr (B == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(gmem), "n"(B)
-                     : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 constexpr int kRowBoundary = 1 << 30;   // pass A's per-row count word: v has a boundary face
 
 // Pass A's shared memory: the fields that do not depend on the mask width
@@ -680,7 +661,7 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
     //     and row counts, and the lists run with every lane busy.  A window
     //     with more first-cell faces than the face list holds handles its
     //     faces entry by entry.
-    const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft;
+    const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft || b.fv || b.ff_off;
     int *pairs = S.work;   // <= 3 per entry
     int *faces = S.cnt;    // <= kCapB, else the fallback below
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -720,21 +701,15 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
         const int ko = cand_of(o, sv);
         const int ka = ko == 0 ? 1 : 0, kb = ko == 2 ? 1 : 2;
         const M mf = S.cm[e][ka] & S.cm[e][kb];
-        const int fid = rank_of(b.frank, 4LL * c + (3 - o));
-        if (b.tf) b.tf[4LL * c + (3 - o)] = fid;
         const M m2 = mf & (mf - 1);
-        if (!m2) {
-            if (b.ft) b.ft[2LL * fid + 1] = -1;
-            return;
-        }
-        const int j2 = rs + mctz(m2);
-        const int c2 = S.cell[j2];
-        if (b.ft) b.ft[2LL * fid + 1] = c2;
-        if (b.tf) {
-            int x, y;
-            face_others(S.tv[e], sv, o, x, y);
-            b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], S.vid[e], x, y))] = fid;
-        }
+        const int j2 = m2 ? rs + mctz(m2) : -1;
+        const int c2 = m2 ? S.cell[j2] : -1;
+        const int v = S.vid[e];
+        int x, y;
+        face_others(S.tv[e], sv, o, x, y);
+        const int fid = face_at_first(b.frank, b.brank, b.tf, b.fv, b.ft, b.ff_off,
+                                      4LL * c + (3 - o), c, c2, v, x, y);
+        if (m2 && b.tf) b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], v, x, y))] = fid;
     };
     if (n_faces <= kCapB) {
         for (int i = threadIdx.x; i < n_faces; i += blockDim.x) face(faces[i] >> 2, faces[i] & 3);
@@ -767,41 +742,6 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
         }
     }
     star_b_body(*reinterpret_cast<StageM<unsigned> *>(raw), b);
-}
-
-// The faces in id order, one thread per face occurrence q = 4 cell + col (a
-// warp covers eight cells): a first occurrence (its bit in fflag) gets its id
-// from the rank words and writes FV, FT's first cell and the FF offset
-// (3 * (2 * id - boundary faces before it)); consecutive lanes holding faces
-// write consecutive ids.
-__global__ void __launch_bounds__(256)
-k_face_slots(const uint32_t *__restrict__ fflag, const uint2 *__restrict__ frank,
-             const uint2 *__restrict__ brank, const int4 *__restrict__ tvs, int64_t T,
-             int *__restrict__ fv, int *__restrict__ ft, int64_t *__restrict__ ff_off)
-{
-    griddep_wait();
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= 4 * T) return;
-    const uint32_t word = __ldg(fflag + (q >> 5));
-    const int b = (int)(q & 31);
-    if (!((word >> b) & 1u)) return;
-    const uint2 fr = __ldg(frank + (q >> 5));
-    const int fid = (int)fr.y + __popc(word & ((1u << b) - 1u));
-    const int64_t c = q >> 2;
-    const int col = (int)(q & 3);
-    if (fv) {
-        // the face omits slot 3 - col
-        const int4 w = __ldg(tvs + c);
-        fv[3LL * fid] = col == 3 ? w.y : w.x;
-        fv[3LL * fid + 1] = col >= 2 ? w.z : w.y;
-        fv[3LL * fid + 2] = col >= 1 ? w.w : w.z;
-    }
-    if (ft) ft[2LL * fid] = (int)c;
-    if (ff_off) {
-        const uint2 br = __ldg(brank + (q >> 5));
-        const int nb = (int)br.y + __popc(br.x & ((1u << b) - 1u));
-        ff_off[fid] = 3LL * (2LL * fid - nb);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1241,16 +1181,6 @@ void launch_star_a(const StarA &a, cudaStream_t s)
         launch_pdl(k_star_a<uint32_t>, n_windows(a.nvt), kThreads, 0, s, a);
     else
         launch_pdl(k_star_a<uint64_t>, n_windows(a.nvt), kThreads, 0, s, a);
-}
-
-void launch_face_slots(const uint32_t *fflag, const uint2 *frank, const uint2 *brank,
-                       const int4 *tvs, int64_t T, int32_t *fv, int32_t *ft, int64_t *ff_off,
-                       cudaStream_t s)
-{
-    if (T == 0) return;
-    Launch L("k_face_slots", s);
-    launch_pdl(k_face_slots, (unsigned)((4 * T + 255) / 256), 256, 0, s, fflag, frank, brank,
-               tvs, T, fv, ft, ff_off);
 }
 
 void launch_star_b(const StarB &b, cudaStream_t s)
