@@ -589,8 +589,10 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         // ---- pass B: ids, VV, fixed-width relations, ET rows ----
         const bool need_ev = mask & (TG_EV | TG_EE | TG_EF);
         const bool need_te = mask & (TG_TE | TG_FE);
-        const bool need_tf = (mask & (TG_TF | TG_FE | TG_FF | TG_EF)) || want_tt_face;
-        const bool need_ft = (mask & (TG_FT | TG_FE | TG_FF)) || want_tt_face;
+        // FV and FE are written at each face's first cell (k_cell_fe_tt), which
+        // the cell's TF row and the face's FT row tell
+        const bool need_tf = (mask & (TG_TF | TG_FV | TG_FE | TG_FF | TG_EF)) || want_tt_face;
+        const bool need_ft = (mask & (TG_FT | TG_FV | TG_FE | TG_FF)) || want_tt_face;
         int32_t *vv, *eid_sorted = nullptr;
         int32_t *ev = nullptr, *te = nullptr, *tf = nullptr, *fv = nullptr, *ft = nullptr;
         int64_t *ff_off = nullptr;
@@ -608,8 +610,6 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (mask & TG_EE) TRY(tmp.alloc(&eid_sorted, nvv));
         if (need_te) TRY(tmp.alloc(&te, 6 * T));
         if (need_tf) TRY(tmp.alloc(&tf, 4 * T));
-        // FV, FT and the FF offsets are written by pass B at each face's
-        // first cell
         if (mask & TG_FV) TRY(tmp.alloc(&fv, 3 * F));
         if (need_ft) TRY(tmp.alloc(&ft, 2 * F));
         if (mask & TG_FF) TRY(tmp.alloc(&ff_off, F + 1));
@@ -639,7 +639,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
         b.emask = emask; b.narrow = narrow; b.vv = vv; b.eid_sorted = eid_sorted;
-        b.te = te; b.tf = tf; b.ft = ft; b.fv = fv; b.ff_off = ff_off;
+        b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.st = m->st;
         launch_star_b(b, s);
         if (m->n_heavy > 0) {
@@ -649,11 +649,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             hv.vv = vv;
             hv.eid_sorted = eid_sorted;
             hv.te = te;
-            hv.brank = brank;
             hv.tf = tf;
             hv.ft = ft;
-            hv.fv = fv;
-            hv.ff_off = ff_off;
             hv.et = et;
             hv.et_off = et_off;
             launch_heavy_b(hv, s);
@@ -673,12 +670,12 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (ee_off) TRY(dalloc(&ee, n_ee, s));
         const bool prep_adj = (opts & TG_OPT_LINK_ADJACENCY) && (mask & TG_VV);
         if (prep_adj) TRY(dalloc(&m->cadj, nvv, s));
-        if (fe || tt || ff_off || ff || ef || prep_adj) {
+        if (fv || fe || tt || ff_off || ff || ef || prep_adj) {
             const cudaStream_t s2 = side.fork();
             if (ef) launch_ef_fill(ev, E, et_off, et, m->tvs, tf, ef_off, ef, s2);
-            if (fe || tt || ff_off)
-                launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fe, tt_off, tt, ff_off, s2);
-            if (ff) launch_ff_fill(ft, tf, F, ff_off, ff, s2);
+            if (fv || fe || tt || ff_off)
+                launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fv, fe, tt_off, tt, ff_off, s2);
+            if (ff) launch_ff_fill(ft, tf, brank, F, ff_off, ff, s2);
             if (prep_adj) TRY(build_link_adjacency(m, vv_off, vv, nvv, tmp, s2));
         }
         if (ee_off) {

@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
                 h.te[6LL * c + pair_slot(sv, t)] = id_at[lo];
             }
         }
-        if (sv > 1 || (!h.tf && !h.ft && !h.fv && !h.ff_off)) continue;
+        if (sv > 1 || (!h.tf && !h.ft)) continue;
         const int o_lo = sv == 0 ? 1 : 0, o_hi = sv == 0 ? 3 : 0;
         for (int o = o_lo; o <= o_hi; o++) {
             int x, y, x0, x1, y0, y1, f1, f2;
@@ -325,8 +325,7 @@ __global__ void __launch_bounds__(64) k_heavy_b(HeavyStars h)
             if (f1 != j) continue;
             const long long q = 4LL * c + (3 - o);
             const int c2 = f2 < 0 ? -1 : s.cells[f2];
-            const int fid = face_at_first(h.frank, h.brank, h.tf, h.fv, h.ft, h.ff_off, q, c, c2,
-                                          v, x, y);
+            const int fid = face_at_first(h.frank, h.tf, h.ft, q, c, c2);
             if (c2 >= 0 && h.tf) h.tf[4LL * c2 + (3 - omitted_slot(h.tvs[c2], v, x, y))] = fid;
         }
     }

@@ -247,53 +247,39 @@ struct StarB {
     int32_t *te;               // [6T] or null
     int32_t *tf;               // [4T] or null
     int32_t *ft;               // [2F] or null
-    int32_t *fv;               // [3F] or null
-    int64_t *ff_off;           // [F + 1] or null: FF offsets but the closing one
     const int64_t *et_off;
     int32_t *et;               // or null
     DevStatus *st;
 };
 void launch_star_b(const StarB &b, cudaStream_t s);
 
-// A face at its first cell c (occurrence q = 4c + TF column), owned by its
-// lowest vertex v, the others x < y, c2 its second cell or -1: its id is the
-// rank of q among first occurrences, and the face's FV row, FT row, FF
-// offset (3 * (2 * id - boundary faces before it)) and TF entry in c are
-// written here; the caller writes TF in c2.  Pass B and the heavy-star pass
-// call it, once per face.
-__device__ __forceinline__ int face_at_first(const uint2 *__restrict__ frank,
-                                             const uint2 *__restrict__ brank, int32_t *tf,
-                                             int32_t *fv, int32_t *ft, int64_t *ff_off,
-                                             long long q, int c, int c2, int v, int x, int y)
+// A face at its first cell c (occurrence q = 4c + TF column), c2 its
+// second cell or -1: its id is the rank of q among first occurrences; its
+// FT row and its TF entry in c are written here, the caller writes TF in c2.
+// Pass B and the heavy-star pass call it, once per face (FV and FE follow
+// at the first cell in k_cell_fe_tt, the FF offset in k_ff_fill).
+__device__ __forceinline__ int face_at_first(const uint2 *__restrict__ frank, int32_t *tf,
+                                             int32_t *ft, long long q, int c, int c2)
 {
     const uint2 w = __ldg(frank + (q >> 5));
-    const unsigned below = (1u << (q & 31)) - 1u;
-    const int fid = (int)w.y + __popc(w.x & below);
+    const int fid = (int)w.y + __popc(w.x & ((1u << (q & 31)) - 1u));
     if (tf) tf[q] = fid;
-    if (fv) {
-        fv[3LL * fid] = v;
-        fv[3LL * fid + 1] = x;
-        fv[3LL * fid + 2] = y;
-    }
     if (ft) *reinterpret_cast<int2 *>(ft + 2LL * fid) = make_int2(c, c2);
-    if (ff_off) {
-        const uint2 bw = __ldg(brank + (q >> 5));
-        ff_off[fid] = 3LL * (2LL * fid - ((long long)bw.y + __popc(bw.x & below)));
-    }
     return fid;
 }
 
-// FE of every face at its first cell; TT offsets (4c - boundary faces before
-// cell c), TT rows, and the closing FF offset.
+// FV and FE of every face at its first cell; TT offsets (4c - boundary faces
+// before cell c), TT rows, and the closing FF offset.
 void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
-                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fe,
-                       int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
+                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fv,
+                       int32_t *fe, int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
 // EF rows (one thread per edge) from ET, the sorted TV and TF
 void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const int32_t *et,
                     const int4 *tvs, const int32_t *tf, const int64_t *ef_off, int32_t *ef,
                     cudaStream_t s);
-void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64_t *ff_off,
-                    int32_t *ff, cudaStream_t s);
+// FF offsets (but the closing one) and rows
+void launch_ff_fill(const int32_t *ft, const int32_t *tf, const uint2 *brank, int64_t F,
+                    int64_t *ff_off, int32_t *ff, cudaStream_t s);
 void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const int32_t *eid_sorted,
                     const int64_t *ee_off, int32_t *ee, cudaStream_t s);
 void launch_tt_vertex_count(const int4 *tvs, int64_t T, const int64_t *vt_off, const int32_t *vt,
@@ -319,9 +305,8 @@ struct HeavyStars {
     uint32_t *ecnt, *eflag, *fflag, *fbnd;
     // pass B
     const int64_t *vv_off;
-    const uint2 *erank, *frank, *brank;
-    int32_t *vv, *eid_sorted, *te, *tf, *ft, *fv, *et;
-    int64_t *ff_off;
+    const uint2 *erank, *frank;
+    int32_t *vv, *eid_sorted, *te, *tf, *ft, *et;
     const int64_t *et_off;
 };
 void launch_heavy_a(const HeavyStars &h, cudaStream_t s);

@@ -196,8 +196,8 @@ __device__ __forceinline__ int rank_of(const uint2 *__restrict__ rk, long long p
 __global__ void __launch_bounds__(256)
 k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__restrict__ te,
              const int *__restrict__ tf, const int *__restrict__ ft, const uint2 *__restrict__ brank,
-             int *__restrict__ fe, int64_t *__restrict__ tt_off, int *__restrict__ tt,
-             int64_t *__restrict__ ff_off)
+             int *__restrict__ fv, int *__restrict__ fe, int64_t *__restrict__ tt_off,
+             int *__restrict__ tt, int64_t *__restrict__ ff_off)
 {
     griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -208,22 +208,31 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__re
         if (ff_off) ff_off[F] = 3 * (2 * F - nb);
     }
     const int4 f4 = reinterpret_cast<const int4 *>(tf)[c];
+    const int4 w = fv ? tvs[c] : make_int4(0, 0, 0, 0);
     int nbr[4];
     int n = 0;
 #pragma unroll
     for (int col = 0; col < 4; col++) {
         const int f = get4(f4, col);
         const int2 cells = reinterpret_cast<const int2 *>(ft)[f];
-        if (fe && cells.x == (int)c) {
+        if (cells.x == (int)c) {
+            // the face's first cell: its vertices omit slot 3 - col
             const int omit = 3 - col;
             int sl[3], k = 0;
 #pragma unroll
             for (int t = 0; t < 4; t++)
                 if (t != omit) sl[k++] = t;
-            const int *row = te + 6 * c;
-            fe[3LL * f] = row[pair_slot(sl[0], sl[1])];
-            fe[3LL * f + 1] = row[pair_slot(sl[0], sl[2])];
-            fe[3LL * f + 2] = row[pair_slot(sl[1], sl[2])];
+            if (fv) {
+                fv[3LL * f] = get4(w, sl[0]);
+                fv[3LL * f + 1] = get4(w, sl[1]);
+                fv[3LL * f + 2] = get4(w, sl[2]);
+            }
+            if (fe) {
+                const int *row = te + 6 * c;
+                fe[3LL * f] = row[pair_slot(sl[0], sl[1])];
+                fe[3LL * f + 1] = row[pair_slot(sl[0], sl[2])];
+                fe[3LL * f + 2] = row[pair_slot(sl[1], sl[2])];
+            }
         }
         const int o = (cells.x == (int)c) ? cells.y : cells.x;
         nbr[col] = o >= 0 ? o : INT_MAX;   // no cell across a boundary face
@@ -289,12 +298,14 @@ k_ef_fill(const int2 *__restrict__ ev, int64_t E, const int64_t *__restrict__ et
 }
 
 __global__ void __launch_bounds__(256)
-k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
-          const int64_t *__restrict__ ff_off, int *__restrict__ ff)
+k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, const uint2 *__restrict__ brank,
+          int64_t F, int64_t *__restrict__ ff_off, int *__restrict__ ff)
 {
     griddep_wait();
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
+    // the offset: 3 * (2 f - boundary faces before f), the boundary faces
+    // counted over occurrence slots up to f's first one (4 cell + column)
     // the faces of the face's two cells, f itself (once in each row) and a
     // missing second cell as INT_MAX, sorted by a 19-comparator network: the
     // first 6 (interior) or 3 (boundary) are the row
@@ -302,6 +313,9 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
     const int4 w0 = reinterpret_cast<const int4 *>(tf)[cells.x];
     const int4 w1 = cells.y >= 0 ? reinterpret_cast<const int4 *>(tf)[cells.y]
                                  : make_int4((int)f, (int)f, (int)f, (int)f);
+    const int col = w0.x == (int)f ? 0 : (w0.y == (int)f ? 1 : (w0.z == (int)f ? 2 : 3));
+    const int64_t off = 3 * (2 * f - rank_of(brank, 4LL * cells.x + col));
+    ff_off[f] = off;
     int r[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
     for (int k = 0; k < 8; k++)
@@ -313,7 +327,7 @@ k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, int64_t F,
     cswap(r[1], r[4]); cswap(r[3], r[6]);
     cswap(r[1], r[2]); cswap(r[3], r[4]); cswap(r[5], r[6]);
     const int n = cells.y >= 0 ? 6 : 3;
-    int *row = ff + ff_off[f];
+    int *row = ff + off;
 #pragma unroll
     for (int i = 0; i < 6; i++)
         if (i < n) row[i] = r[i];
@@ -687,14 +701,14 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
 
 
 void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
-                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fe,
-                       int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s)
+                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fv,
+                       int32_t *fe, int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s)
 {
     if (T == 0) return;
     {
         Launch L("k_cell_fe_tt", s);
-        launch_pdl(k_cell_fe_tt, blocks_for(T, 256), 256, 0, s, tvs, T, F, te, tf, ft, brank, fe, tt_off,
-                                                         tt, ff_off);
+        launch_pdl(k_cell_fe_tt, blocks_for(T, 256), 256, 0, s, tvs, T, F, te, tf, ft, brank, fv,
+                   fe, tt_off, tt, ff_off);
     }
 }
 
@@ -708,13 +722,13 @@ void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const i
                et_off, et, tvs, tf, ef_off, ef);
 }
 
-void launch_ff_fill(const int32_t *ft, const int32_t *tf, int64_t F, const int64_t *ff_off,
-                    int32_t *ff, cudaStream_t s)
+void launch_ff_fill(const int32_t *ft, const int32_t *tf, const uint2 *brank, int64_t F,
+                    int64_t *ff_off, int32_t *ff, cudaStream_t s)
 {
     if (F == 0) return;
     {
         Launch L("k_ff_fill", s);
-        launch_pdl(k_ff_fill, blocks_for(F, 256), 256, 0, s, ft, tf, F, ff_off, ff);
+        launch_pdl(k_ff_fill, blocks_for(F, 256), 256, 0, s, ft, tf, brank, F, ff_off, ff);
     }
 }
 

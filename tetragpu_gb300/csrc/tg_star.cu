@@ -30,7 +30,7 @@
 //             neighbour counts, the candidate masks
 //   k_star_b  ids (ranks of first occurrences), sorted VV rows, id-sorted
 //             incident edge ids, TE, TF, ET rows, and at each face's first
-//             cell its FV row, FT row and FF offset
+//             cell its FT row
 //   k_edge_offsets  the id-ordered pass over edge occurrence slots: ET / EF /
 //             EE offsets and EV (one pass with a look-back scan)
 #include "tg_internal.h"
@@ -661,7 +661,7 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
     //     and row counts, and the lists run with every lane busy.  A window
     //     with more first-cell faces than the face list holds handles its
     //     faces entry by entry.
-    const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft || b.fv || b.ff_off;
+    const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft;
     int *pairs = S.work;   // <= 3 per entry
     int *faces = S.cnt;    // <= kCapB, else the fallback below
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -704,12 +704,12 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
         const M m2 = mf & (mf - 1);
         const int j2 = m2 ? rs + mctz(m2) : -1;
         const int c2 = m2 ? S.cell[j2] : -1;
-        const int v = S.vid[e];
-        int x, y;
-        face_others(S.tv[e], sv, o, x, y);
-        const int fid = face_at_first(b.frank, b.brank, b.tf, b.fv, b.ft, b.ff_off,
-                                      4LL * c + (3 - o), c, c2, v, x, y);
-        if (m2 && b.tf) b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], v, x, y))] = fid;
+        const int fid = face_at_first(b.frank, b.tf, b.ft, 4LL * c + (3 - o), c, c2);
+        if (m2 && b.tf) {
+            int x, y;
+            face_others(S.tv[e], sv, o, x, y);
+            b.tf[4LL * c2 + (3 - omitted_slot(S.tv[j2], S.vid[e], x, y))] = fid;
+        }
     };
     if (n_faces <= kCapB) {
         for (int i = threadIdx.x; i < n_faces; i += blockDim.x) face(faces[i] >> 2, faces[i] & 3);
