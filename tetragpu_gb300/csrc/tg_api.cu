@@ -589,8 +589,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         // ---- pass B: ids, VV, fixed-width relations, ET rows ----
         const bool need_ev = mask & (TG_EV | TG_EE | TG_EF);
         const bool need_te = mask & (TG_TE | TG_FE);
-        // FV and FE are written at each face's first cell (k_cell_fe_tt), which
-        // the cell's TF row and the face's FT row tell
+        // FV and FE are read off each face's first cell (k_face_fill), which
+        // the face's FT row and the cell's TF row tell
         const bool need_tf = (mask & (TG_TF | TG_FV | TG_FE | TG_FF | TG_EF)) || want_tt_face;
         const bool need_ft = (mask & (TG_FT | TG_FV | TG_FE | TG_FF)) || want_tt_face;
         int32_t *vv, *eid_sorted = nullptr;
@@ -673,9 +673,8 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         if (fv || fe || tt || ff_off || ff || ef || prep_adj) {
             const cudaStream_t s2 = side.fork();
             if (ef) launch_ef_fill(ev, E, et_off, et, m->tvs, tf, ef_off, ef, s2);
-            if (fv || fe || tt || ff_off)
-                launch_cell_fe_tt(m->tvs, T, F, te, tf, ft, brank, fv, fe, tt_off, tt, ff_off, s2);
-            if (ff) launch_ff_fill(ft, tf, brank, F, ff_off, ff, s2);
+            if (tt || ff_off) launch_cell_tt(T, F, tf, ft, brank, tt_off, tt, ff_off, s2);
+            if (fv || fe || ff) launch_face_fill(ft, tf, m->tvs, te, brank, F, fv, fe, ff_off, ff, s2);
             if (prep_adj) TRY(build_link_adjacency(m, vv_off, vv, nvv, tmp, s2));
         }
         if (ee_off) {

@@ -257,7 +257,7 @@ void launch_star_b(const StarB &b, cudaStream_t s);
 // second cell or -1: its id is the rank of q among first occurrences; its
 // FT row and its TF entry in c are written here, the caller writes TF in c2.
 // Pass B and the heavy-star pass call it, once per face (FV and FE follow
-// at the first cell in k_cell_fe_tt, the FF offset in k_ff_fill).
+// and the FF offset in k_face_fill).
 __device__ __forceinline__ int face_at_first(const uint2 *__restrict__ frank, int32_t *tf,
                                              int32_t *ft, long long q, int c, int c2)
 {
@@ -268,18 +268,19 @@ __device__ __forceinline__ int face_at_first(const uint2 *__restrict__ frank, in
     return fid;
 }
 
-// FV and FE of every face at its first cell; TT offsets (4c - boundary faces
-// before cell c), TT rows, and the closing FF offset.
-void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
-                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fv,
-                       int32_t *fe, int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
+// TT offsets (4c - boundary faces before cell c), TT rows (or null), and the
+// closing TT and FF offsets.
+void launch_cell_tt(int64_t T, int64_t F, const int32_t *tf, const int32_t *ft, const uint2 *brank,
+                    int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s);
 // EF rows (one thread per edge) from ET, the sorted TV and TF
 void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const int32_t *et,
                     const int4 *tvs, const int32_t *tf, const int64_t *ef_off, int32_t *ef,
                     cudaStream_t s);
-// FF offsets (but the closing one) and rows
-void launch_ff_fill(const int32_t *ft, const int32_t *tf, const uint2 *brank, int64_t F,
-                    int64_t *ff_off, int32_t *ff, cudaStream_t s);
+// per face (each may be null): FV, FE, FF offsets (but the closing one) and
+// FF rows (ff_off and ff together)
+void launch_face_fill(const int32_t *ft, const int32_t *tf, const int4 *tvs, const int32_t *te,
+                      const uint2 *brank, int64_t F, int32_t *fv, int32_t *fe, int64_t *ff_off,
+                      int32_t *ff, cudaStream_t s);
 void launch_ee_fill(const int32_t *ev, int64_t E, const int64_t *vv_off, const int32_t *eid_sorted,
                     const int64_t *ee_off, int32_t *ee, cudaStream_t s);
 void launch_tt_vertex_count(const int4 *tvs, int64_t T, const int64_t *vt_off, const int32_t *vt,

@@ -19,8 +19,9 @@
 //   k_vt_fill      scatter cells into VT rows (atomic cursors)
 //   k_sort_rows    sort each CSR row in place (VT, incident-edge rows)
 //   k_star_a/b/c   the per-vertex star passes (tg_star.cu)
-//   k_cell_fe_tt   FE (from TE of a face's first cell) and face-sharing TT
-//   k_ef_fill      EF from ET and TF;  k_ff_fill  FF;  k_ee_fill  EE;
+//   k_cell_tt      face-sharing TT
+//   k_face_fill    FV, FE (from TE of a face's first cell), FF
+//   k_ef_fill      EF from ET and TF;  k_ee_fill  EE;
 //   k_tt_vertex_*  vertex-sharing TT
 #include <algorithm>
 #include <climits>
@@ -190,14 +191,13 @@ __device__ __forceinline__ int rank_of(const uint2 *__restrict__ rk, long long p
     return (int)w.y + __popc(w.x & ((1u << (p & 31)) - 1u));
 }
 
-// FE of each face at its first cell (FT[f][0] == c); TT rows at offset
-// 4c - (boundary faces in cells before c), since a cell's TT row holds one
-// entry per interior face; the closing offsets of TT and FF.
+// Face-sharing TT rows at offset 4c - (boundary faces in cells before c),
+// since a cell's TT row holds one entry per interior face (the cell across
+// each face from FT, sorted); the closing offsets of TT and FF.
 __global__ void __launch_bounds__(256)
-k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__restrict__ te,
-             const int *__restrict__ tf, const int *__restrict__ ft, const uint2 *__restrict__ brank,
-             int *__restrict__ fv, int *__restrict__ fe, int64_t *__restrict__ tt_off,
-             int *__restrict__ tt, int64_t *__restrict__ ff_off)
+k_cell_tt(int64_t T, int64_t F, const int *__restrict__ tf, const int *__restrict__ ft,
+          const uint2 *__restrict__ brank, int64_t *__restrict__ tt_off, int *__restrict__ tt,
+          int64_t *__restrict__ ff_off)
 {
     griddep_wait();
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -207,52 +207,30 @@ k_cell_fe_tt(const int4 *__restrict__ tvs, int64_t T, int64_t F, const int *__re
         if (tt_off) tt_off[T] = 4 * T - nb;
         if (ff_off) ff_off[F] = 3 * (2 * F - nb);
     }
+    if (!tt) return;
     const int4 f4 = reinterpret_cast<const int4 *>(tf)[c];
-    const int4 w = fv ? tvs[c] : make_int4(0, 0, 0, 0);
     int nbr[4];
     int n = 0;
 #pragma unroll
     for (int col = 0; col < 4; col++) {
-        const int f = get4(f4, col);
-        const int2 cells = reinterpret_cast<const int2 *>(ft)[f];
-        if (cells.x == (int)c) {
-            // the face's first cell: its vertices omit slot 3 - col
-            const int omit = 3 - col;
-            int sl[3], k = 0;
-#pragma unroll
-            for (int t = 0; t < 4; t++)
-                if (t != omit) sl[k++] = t;
-            if (fv) {
-                fv[3LL * f] = get4(w, sl[0]);
-                fv[3LL * f + 1] = get4(w, sl[1]);
-                fv[3LL * f + 2] = get4(w, sl[2]);
-            }
-            if (fe) {
-                const int *row = te + 6 * c;
-                fe[3LL * f] = row[pair_slot(sl[0], sl[1])];
-                fe[3LL * f + 1] = row[pair_slot(sl[0], sl[2])];
-                fe[3LL * f + 2] = row[pair_slot(sl[1], sl[2])];
-            }
-        }
+        const int2 cells = reinterpret_cast<const int2 *>(ft)[get4(f4, col)];
         const int o = (cells.x == (int)c) ? cells.y : cells.x;
         nbr[col] = o >= 0 ? o : INT_MAX;   // no cell across a boundary face
         n += o >= 0;
     }
-    if (tt) {
-        // a sorting network (no data-dependent loops); the missing
-        // neighbours sort last
-        cswap(nbr[0], nbr[1]);
-        cswap(nbr[2], nbr[3]);
-        cswap(nbr[0], nbr[2]);
-        cswap(nbr[1], nbr[3]);
-        cswap(nbr[1], nbr[2]);
-        const int64_t off = 4 * c - rank_of(brank, 4 * c);
-        tt_off[c] = off;
-        int *row = tt + off;
+    // a sorting network (no data-dependent loops); the missing neighbours
+    // sort last
+    cswap(nbr[0], nbr[1]);
+    cswap(nbr[2], nbr[3]);
+    cswap(nbr[0], nbr[2]);
+    cswap(nbr[1], nbr[3]);
+    cswap(nbr[1], nbr[2]);
+    const int64_t off = 4 * c - rank_of(brank, 4 * c);
+    tt_off[c] = off;
+    int *row = tt + off;
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (i < n) row[i] = nbr[i];
-    }
+    for (int i = 0; i < 4; i++)
+        if (i < n) row[i] = nbr[i];
 }
 
 // EF rows, a thread per edge e = (a, b): walk its ET row (cells ascending)
@@ -297,25 +275,48 @@ k_ef_fill(const int2 *__restrict__ ev, int64_t E, const int64_t *__restrict__ et
     }
 }
 
+// Thread per face f (consecutive threads write consecutive rows): its first
+// cell c (FT[f][0]) and its column in c's TF row give the face's occurrence
+// slot q = 4c + column and its vertices (c's sorted slots but 3 - column);
+// FV from c's vertices, FE from c's TE row, the FF offset 3 * (2f - boundary
+// faces before f, counted over occurrence slots up to q) and the FF row (the
+// faces of both cells, f itself (once in each row) and a missing second
+// cell as INT_MAX, sorted by a 19-comparator network: the first 6 (interior)
+// or 3 (boundary) are the row).
 __global__ void __launch_bounds__(256)
-k_ff_fill(const int *__restrict__ ft, const int *__restrict__ tf, const uint2 *__restrict__ brank,
-          int64_t F, int64_t *__restrict__ ff_off, int *__restrict__ ff)
+k_face_fill(const int *__restrict__ ft, const int *__restrict__ tf, const int4 *__restrict__ tvs,
+            const int *__restrict__ te, const uint2 *__restrict__ brank, int64_t F,
+            int *__restrict__ fv, int *__restrict__ fe, int64_t *__restrict__ ff_off,
+            int *__restrict__ ff)
 {
     griddep_wait();
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
-    // the offset: 3 * (2 f - boundary faces before f), the boundary faces
-    // counted over occurrence slots up to f's first one (4 cell + column)
-    // the faces of the face's two cells, f itself (once in each row) and a
-    // missing second cell as INT_MAX, sorted by a 19-comparator network: the
-    // first 6 (interior) or 3 (boundary) are the row
     const int2 cells = reinterpret_cast<const int2 *>(ft)[f];
     const int4 w0 = reinterpret_cast<const int4 *>(tf)[cells.x];
-    const int4 w1 = cells.y >= 0 ? reinterpret_cast<const int4 *>(tf)[cells.y]
-                                 : make_int4((int)f, (int)f, (int)f, (int)f);
     const int col = w0.x == (int)f ? 0 : (w0.y == (int)f ? 1 : (w0.z == (int)f ? 2 : 3));
+    if (fv || fe) {
+        // the face's slots in its first cell: all but 3 - col
+        const int omit = 3 - col;
+        const int s0 = omit == 0 ? 1 : 0, s1 = omit <= 1 ? 2 : 1, s2 = omit <= 2 ? 3 : 2;
+        if (fv) {
+            const int4 w = tvs[cells.x];
+            fv[3 * f] = get4(w, s0);
+            fv[3 * f + 1] = get4(w, s1);
+            fv[3 * f + 2] = get4(w, s2);
+        }
+        if (fe) {
+            const int *row = te + 6LL * cells.x;
+            fe[3 * f] = row[pair_slot(s0, s1)];
+            fe[3 * f + 1] = row[pair_slot(s0, s2)];
+            fe[3 * f + 2] = row[pair_slot(s1, s2)];
+        }
+    }
+    if (!ff) return;
     const int64_t off = 3 * (2 * f - rank_of(brank, 4LL * cells.x + col));
     ff_off[f] = off;
+    const int4 w1 = cells.y >= 0 ? reinterpret_cast<const int4 *>(tf)[cells.y]
+                                 : make_int4((int)f, (int)f, (int)f, (int)f);
     int r[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
     for (int k = 0; k < 8; k++)
@@ -700,15 +701,14 @@ void launch_sort_rows(const int64_t *off, int32_t *ent, int64_t n_rows, cudaStre
 
 
 
-void launch_cell_fe_tt(const int4 *tvs, int64_t T, int64_t F, const int32_t *te,
-                       const int32_t *tf, const int32_t *ft, const uint2 *brank, int32_t *fv,
-                       int32_t *fe, int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s)
+void launch_cell_tt(int64_t T, int64_t F, const int32_t *tf, const int32_t *ft, const uint2 *brank,
+                    int64_t *tt_off, int32_t *tt, int64_t *ff_off, cudaStream_t s)
 {
     if (T == 0) return;
     {
-        Launch L("k_cell_fe_tt", s);
-        launch_pdl(k_cell_fe_tt, blocks_for(T, 256), 256, 0, s, tvs, T, F, te, tf, ft, brank, fv,
-                   fe, tt_off, tt, ff_off);
+        Launch L("k_cell_tt", s);
+        launch_pdl(k_cell_tt, blocks_for(T, 256), 256, 0, s, T, F, tf, ft, brank, tt_off, tt,
+                   ff_off);
     }
 }
 
@@ -722,13 +722,15 @@ void launch_ef_fill(const int32_t *ev, int64_t E, const int64_t *et_off, const i
                et_off, et, tvs, tf, ef_off, ef);
 }
 
-void launch_ff_fill(const int32_t *ft, const int32_t *tf, const uint2 *brank, int64_t F,
-                    int64_t *ff_off, int32_t *ff, cudaStream_t s)
+void launch_face_fill(const int32_t *ft, const int32_t *tf, const int4 *tvs, const int32_t *te,
+                      const uint2 *brank, int64_t F, int32_t *fv, int32_t *fe, int64_t *ff_off,
+                      int32_t *ff, cudaStream_t s)
 {
     if (F == 0) return;
     {
-        Launch L("k_ff_fill", s);
-        launch_pdl(k_ff_fill, blocks_for(F, 256), 256, 0, s, ft, tf, brank, F, ff_off, ff);
+        Launch L("k_face_fill", s);
+        launch_pdl(k_face_fill, blocks_for(F, 256), 256, 0, s, ft, tf, tvs, te, brank, F, fv, fe,
+                   ff_off, ff);
     }
 }
 
