@@ -456,7 +456,9 @@ template <typename G>
 __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 {
     griddep_wait();
-    __shared__ __align__(16) unsigned char raw[sizeof(Stage<unsigned long long>)];
+    // sized for the widest masks this instantiation uses (32-bit ones leave
+    // room for larger windows at eight blocks per SM)
+    __shared__ __align__(16) unsigned char raw[sizeof(Stage<G>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
     if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.vtp, a.tvs, a.st)) return;
@@ -732,7 +734,7 @@ template <typename G>
 __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
 {
     griddep_wait();
-    __shared__ __align__(16) unsigned char raw[sizeof(StageM<unsigned long long>)];
+    __shared__ __align__(16) unsigned char raw[sizeof(StageM<G>)];
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
     stage_rows_b(raw, b, static_cast<const G *>(b.emask));
     if constexpr (sizeof(G) == 8) {
