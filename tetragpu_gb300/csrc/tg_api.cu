@@ -158,7 +158,7 @@ struct PinnedPool {
 PinnedPool g_pinned;
 
 // Side streams for kernels of one extraction that need nothing from each
-// other (the face slots beside the edge offsets; FE / TT and FF beside EE):
+// other (EF, TT, the per-face rows and the link adjacency beside EE):
 // a stream and its fork / join events, kept per device and reused, so that a
 // mesh built per request creates none.
 struct SideLane {
@@ -663,9 +663,10 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
             m->cadj = nullptr;
         }
 
-        // EF, the cell-ordered FE / TT and FF rows, and on request the link
-        // adjacency of critical points, on a side stream beside EE (each
-        // reads only what pass B and the passes before it wrote)
+        // EF, the per-cell TT rows, the per-face FV / FE / FF rows and on
+        // request the link adjacency of critical points, on a side stream
+        // beside EE (each reads only what pass B and the passes before it
+        // wrote)
         const int64_t n_ee = sum_deg_sq - 2 * E;   // deg(a) + deg(b) - 2 per edge (a,b)
         if (ee_off) TRY(dalloc(&ee, n_ee, s));
         const bool prep_adj = (opts & TG_OPT_LINK_ADJACENCY) && (mask & TG_VV);
