@@ -191,11 +191,10 @@ def kernel_bytes(name: str, c: dict, tot: dict) -> int:
     (pass A's candidate masks, the id-sorted incident edges, rank words,
     offsets read back) are overhead and not credited.  k_star_b reads the
     sorted TV (16 B per cell) and writes TE, TF, the ET entries, the VV
-    entries and per face its FV row, FT row and FF offset."""
+    entries and every face's FT row."""
     V, E, F, T = c["V"], c["E"], c["F"], c["T"]
     if name == "k_star_b":
-        return 16 * T + 4 * 6 * T + 4 * 4 * T + 4 * tot["ET"] + 4 * tot["VV"] \
-            + (12 + 8 + 8) * F
+        return 16 * T + 4 * 6 * T + 4 * 4 * T + 4 * tot["ET"] + 4 * tot["VV"] + 8 * F
     raise KeyError(name)
 
 
