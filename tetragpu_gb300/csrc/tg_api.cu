@@ -463,16 +463,17 @@ tg_status build_link_adjacency(tg_mesh *m, const int64_t *vv_off, const int32_t 
 {
     const int64_t V = m->V;
     int32_t *len, *win;
-    int64_t *ooff;
+    int64_t *ooff, *ostart;
     TRY(tmp.alloc(&len, V));
     TRY(tmp.alloc(&ooff, V + 1));
+    TRY(tmp.alloc(&ostart, V));
     TRY(tmp.alloc(&win, window_count(nvv, crit_window()) + 1));
-    launch_vv_lengths_in_order(vv_off, m->vorder, V, m->n_light + m->n_heavy, len, s);
+    launch_vv_lengths_in_order(vv_off, m->vorder, V, m->n_light + m->n_heavy, len, ostart, s);
     ScanJob job{len, ooff, V, SCAN_COUNT_I32, 0};
     scan_batch(&job, 1, m->scan, m->st, s);
     launch_window_starts(ooff, V, nvv, crit_window(), win, s);
-    launch_crit_adj(vv_off, vv, m->vorder, ooff, win, V, nvv, m->cadj, m->st, m->max_deg ? 1 : 0,
-                    s);
+    launch_crit_adj(vv_off, vv, m->vorder, ooff, ostart, win, V, nvv, m->cadj, m->st,
+                    m->max_deg ? 1 : 0, s);
     return TG_OK;
 }
 

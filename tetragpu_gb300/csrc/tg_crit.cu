@@ -94,14 +94,15 @@ __device__ __forceinline__ void adj_scan(const int *row, int d, int top,
 //
 // Windows run over the rows in `order` (the star processing order: vertices
 // by first cell, so consecutive windows share neighbours and the neighbours'
-// rows stay in L2; ooff = the row lengths' prefix in that order), or in id
-// order when order is null (ooff = vv_off).  A staged row keeps its global
-// start in gst[row start].
+// rows stay in L2; ooff = the row lengths' prefix in that order, ostart =
+// each row's start in VV, read beside ooff instead of after the vertex), or
+// in id order when order is null (ooff = vv_off).  A staged row keeps its
+// global start in gst[row start].
 __global__ void __launch_bounds__(kAdjThreads)
 k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64_t n_vv,
            const int *__restrict__ order, const int64_t *__restrict__ ooff,
-           const int *__restrict__ win, unsigned long long *__restrict__ adj, DevStatus *st,
-           int heavy)
+           const int64_t *__restrict__ ostart, const int *__restrict__ win,
+           unsigned long long *__restrict__ adj, DevStatus *st, int heavy)
 {
     griddep_wait();
     __shared__ int nb[kAdjCap];
@@ -143,19 +144,18 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
             }
             continue;
         }
-        gst[rs] = order ? vv_off[v] : base + rs;
+        const long long g0 = order ? ostart[i] : base + rs;
+        gst[rs] = g0;
+        // the row's entries are copied asynchronously as soon as its start
+        // is known
         for (int k = 0; k < d; k++) {
             meta[rs + k] = rs | (d << 16);
             vid[rs + k] = v;
+            cp_async<4>(&nb[rs + k], vv + g0 + k);
         }
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int m = meta[e];
-        if (heavy && m < 0) continue;
-        const int rs = m & 0xffff;
-        nb[e] = __ldg(vv + gst[rs] + (e - rs));
-    }
+    cp_async_commit();
+    cp_async_wait();
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = meta[e];
@@ -269,42 +269,47 @@ k_crit_classify(const int64_t *__restrict__ vv_off, const int *__restrict__ vv,
 int crit_window() { return kAdjWin; }
 
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *order,
-                     const int64_t *ooff, const int32_t *vv_win, int64_t V, int64_t n_vv,
-                     uint64_t *adj, DevStatus *st, int heavy, cudaStream_t s)
+                     const int64_t *ooff, const int64_t *ostart, const int32_t *vv_win,
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, int heavy,
+                     cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_crit_adj", s);
     launch_pdl(k_crit_adj, (unsigned)window_count(n_vv, kAdjWin), kAdjThreads, 0, s,
-        vv_off, vv, n_vv, order, order ? ooff : vv_off, vv_win,
+        vv_off, vv, n_vv, order, order ? ooff : vv_off, ostart, vv_win,
         reinterpret_cast<unsigned long long *>(adj), st, heavy);
 }
 
 namespace {
-// row lengths of VV in the star processing order (positions past the
-// vertices with cells hold placeholders: length 0)
+// row lengths and row starts of VV in the star processing order (positions
+// past the vertices with cells hold placeholders: length 0)
 __global__ void __launch_bounds__(256)
 k_vv_lengths_in_order(const int64_t *__restrict__ vv_off, const int *__restrict__ order,
-                      int64_t V, int64_t n_with_cells, int *__restrict__ len)
+                      int64_t V, int64_t n_with_cells, int *__restrict__ len,
+                      int64_t *__restrict__ start)
 {
     griddep_wait();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     int d = 0;
+    int64_t b = 0;
     if (i < n_with_cells) {
         const int v = order[i];
-        d = (int)(vv_off[v + 1] - vv_off[v]);
+        b = vv_off[v];
+        d = (int)(vv_off[v + 1] - b);
     }
     len[i] = d;
+    start[i] = b;
 }
 }  // namespace
 
 void launch_vv_lengths_in_order(const int64_t *vv_off, const int32_t *order, int64_t V,
-                                int64_t n_with_cells, int32_t *len, cudaStream_t s)
+                                int64_t n_with_cells, int32_t *len, int64_t *start, cudaStream_t s)
 {
     if (V == 0) return;
     Launch L("k_vv_lengths_in_order", s);
     launch_pdl(k_vv_lengths_in_order, (unsigned)((V + 255) / 256), 256, 0, s, vv_off, order, V,
-               n_with_cells, len);
+               n_with_cells, len, start);
 }
 
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,

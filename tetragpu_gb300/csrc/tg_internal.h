@@ -328,15 +328,18 @@ int crit_window();
 // heavy: 0 no row longer than kMaxDeg, 1 such rows get the heavy path
 // (masks of their light neighbours computed from the light side), 2 report
 // them with ST_HEAVY_DEG
-// order / ooff: visit the rows in this vertex order (ooff: the row lengths'
-// prefix in it, V + 1 entries; vv_win a window table over ooff), or null for
-// id order (vv_win over vv_off)
+// order / ooff / ostart: visit the rows in this vertex order (ooff: the row
+// lengths' prefix in it, V + 1 entries; ostart: each row's start in VV;
+// vv_win a window table over ooff), or null for id order (vv_win over vv_off)
 void launch_crit_adj(const int64_t *vv_off, const int32_t *vv, const int32_t *order,
-                     const int64_t *ooff, const int32_t *vv_win, int64_t V, int64_t n_vv,
-                     uint64_t *adj, DevStatus *st, int heavy, cudaStream_t s);
-// len[i] = length of VV row order[i] (0 from n_with_cells on)
+                     const int64_t *ooff, const int64_t *ostart, const int32_t *vv_win,
+                     int64_t V, int64_t n_vv, uint64_t *adj, DevStatus *st, int heavy,
+                     cudaStream_t s);
+// len[i] = length and start[i] = first entry of VV row order[i] (0 from
+// n_with_cells on)
 void launch_vv_lengths_in_order(const int64_t *vv_off, const int32_t *order, int64_t V,
-                                int64_t n_with_cells, int32_t *len, cudaStream_t s);
+                                int64_t n_with_cells, int32_t *len, int64_t *start,
+                                cudaStream_t s);
 // classify rows [v0, v0 + nv): field and classes3 hold nv values / rows from v0
 void launch_crit_classify(const int64_t *vv_off, const int32_t *vv, const uint64_t *adj,
                           const void *field, int field_type, int64_t v0, int64_t nv,

@@ -107,8 +107,8 @@ extern "C" tg_status tg_critical_points_noalloc(const int64_t *vv_off, const int
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(tg::DevStatus), s);
     if (e != cudaSuccess) return fail(TG_ERR_CUDA, "clearing the status word", e);
     tg::launch_window_starts(vv_off, n_verts, n_vv_entries, tg::crit_window(), (int32_t *)win, s);
-    tg::launch_crit_adj(vv_off, vv, nullptr, nullptr, (const int32_t *)win, n_verts, n_vv_entries,
-                        (uint64_t *)adj, (tg::DevStatus *)status, 2, s);
+    tg::launch_crit_adj(vv_off, vv, nullptr, nullptr, nullptr, (const int32_t *)win, n_verts,
+                        n_vv_entries, (uint64_t *)adj, (tg::DevStatus *)status, 2, s);
     tg::launch_crit_classify(vv_off, vv, (const uint64_t *)adj, field, field_type, 0, n_verts,
                              classes_out, s);
     e = cudaGetLastError();

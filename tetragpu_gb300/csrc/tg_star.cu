@@ -136,6 +136,11 @@ struct StageBaseB {
 template <typename M>
 struct StageM : StageBaseB {
     M cm[kCapB][3];                      // star positions holding each candidate
+    // with 32-bit masks, room for each listed neighbour's first occurrence
+    // (6 cell + pair slot): phase 2 then ranks a first sighting among the
+    // row's edge ids (the order of their first occurrences) together with
+    // its VV rank, with no pass rewriting the lists as ids
+    int lkey[sizeof(M) == 4 ? 3 * kCapB : 1];
 };
 static_assert(sizeof(StageM<unsigned long long>) <= 48 * 1024,
               "star stage B exceeds the static shared-memory limit");
@@ -583,9 +588,12 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (mctz(S.cm[e][k]) != pos) continue;
-            const int u = get4(w, k + (k >= sv));
+            const int t = k + (k >= sv);
+            const int u = get4(w, t);
             const int li = atomicAdd(&S.cnt[rs], 1);
             S.list_u[3 * rs + li] = u;
+            if constexpr (sizeof(M) == 4)
+                S.lkey[3 * rs + li] = 6 * S.cell[e] + pair_slot(min(sv, t), max(sv, t));
             S.hv[e][k] = li;
             const int item = (li << 11) | (e << 2) | k;
             if (u > v)
@@ -600,7 +608,29 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
         return i < n_owned ? S.work[i] : S.work[3 * kCapB - 1 - (i - n_owned)];
     };
 
-    // 2. every first sighting: edge id and VV position
+    // 2. every first sighting: edge id and VV position (with 32-bit masks also
+    //    its place among v's incident edge ids, for EE)
+    if constexpr (sizeof(M) == 4) {
+        for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
+            const int it = first_item(i);
+            const int e = (it >> 2) & 511, k = it & 3;
+            const int v = S.vid[e], rs = m_rs(S.meta[e]);
+            const int u = S.list_u[3 * rs + (it >> 11)], p = S.lkey[3 * rs + (it >> 11)];
+            const int deg = S.cnt[rs];
+            const int *lu = S.list_u + 3 * rs, *lk = S.lkey + 3 * rs;
+            int rank = 0, er = 0;
+            for (int j = 0; j < deg; j++) {
+                rank += lu[j] < u;
+                er += lk[j] < p;
+            }
+            const int id = rank_of(b.erank, p);
+            S.hv[e][k] = id;
+            const long long vb = b.vv_off[v];
+            if (b.vv) b.vv[vb + rank] = u;
+            if (b.eid_sorted) b.eid_sorted[vb + er] = id;
+        }
+        __syncthreads();
+    } else {
     for (int i = threadIdx.x; i < n_first; i += blockDim.x) {
         const int it = first_item(i);
         const int e = (it >> 2) & 511, k = it & 3;
@@ -640,6 +670,7 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
             b.eid_sorted[b.vv_off[S.vid[e]] + r] = id;
         }
         __syncthreads();
+    }
     }
     // 3b. the ET offsets of the edges v owns, once per edge, at its first
     //     sighting (in the neighbour lists' space, free from here on; ET
