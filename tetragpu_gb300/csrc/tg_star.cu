@@ -682,7 +682,10 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
             const int e = (it >> 2) & 511, k = it & 3;
             eto[3 * e + k] = (int)b.et_off[S.hv[e][k]];
         }
-        __syncthreads();
+        // with 32-bit masks the pair list below goes to the spent first
+        // occurrences, not over the owned edges this loop reads: no barrier
+        // between the two (the ET offsets' loads stay in flight meanwhile)
+        if constexpr (sizeof(M) != 4) __syncthreads();
     }
     // 3c. TE of the pairs v is the low end of and the entry's cell in those
     //     edges' ET rows (its place: the star positions below it holding the
@@ -690,12 +693,13 @@ __device__ __forceinline__ void star_b_body(StageM<M> &S, const StarB &b)
     //     their first cell.  An entry holds 3 - sv such pairs and, at sv <= 1,
     //     up to three faces, so a loop over entries would leave most lanes
     //     idle; the pairs (entry << 2 | other slot) and the faces (entry << 2
-    //     | omitted slot) are listed first, in the spent first-sighting list
-    //     and row counts, and the lists run with every lane busy.  A window
+    //     | omitted slot) are listed first, in the spent first occurrences (or
+    //     first-sighting list) and row counts, and the lists run with every
+    //     lane busy.  A window
     //     with more first-cell faces than the face list holds handles its
     //     faces entry by entry.
     const bool do_pairs = b.te || b.et, do_faces = b.tf || b.ft;
-    int *pairs = S.work;   // <= 3 per entry
+    int *pairs = sizeof(M) == 4 ? S.lkey : S.work;   // <= 3 per entry
     int *faces = S.cnt;    // <= kCapB, else the fallback below
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
