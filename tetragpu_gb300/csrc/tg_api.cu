@@ -528,7 +528,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         uint32_t *emask;
         TRY(tmp.alloc(&emask, (narrow ? 3 : 6) * NVT));
         StarA a{m->pofs, m->st_win, m->st_wbase, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt,
-                eflag, fflag, fbnd, m->st, emask, narrow};
+                eflag, fflag, fbnd, m->st, emask, narrow, NVT - m->heavy_entries};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));

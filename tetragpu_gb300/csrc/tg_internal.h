@@ -210,6 +210,7 @@ struct StarA {
     DevStatus *st;
     void *emask;               // [3][nvt] star positions holding each entry's candidates
     bool narrow;               // no star holds more than 32 cells: emask is 32-bit, else 64
+    int64_t light_end;         // entries of the light stars (they come first): 4T - heavy entries
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
 // seg_ef[i] = first edge id and seg_ef[n + 1 + i] = first face id of the

@@ -257,14 +257,57 @@ __device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
     return true;
 }
 
+// With 32-bit masks in global memory (every window narrow) the staging needs
+// one barrier: the window ends at the next window's first entry or at the
+// first heavy star's (light_end), each row's thread writes its entries' row
+// metadata itself, and the table's keys and masks are cleared here.
+__device__ void stage_rows_a_narrow(Stage<unsigned> &S, const StarA &a)
+{
+    const int plo = __ldg(a.win + blockIdx.x), phi = __ldg(a.win + blockIdx.x + 1);
+    const int base = __ldg(a.wbase + blockIdx.x);
+    const int n = (int)(min((int64_t)__ldg(a.wbase + blockIdx.x + 1), a.light_end) - base);
+    for (int e = threadIdx.x; e < n; e += blockDim.x) cp_async<4>(&S.cell[e], a.vtp + base + e);
+    cp_async_commit();
+    if (threadIdx.x == 0) {
+        S.vlo = plo;
+        S.vhi = phi;
+        S.base = base;
+        S.n = n;
+        S.full = 0;
+        S.wide = 0;
+    }
+    for (int h = threadIdx.x; h < kHash; h += blockDim.x) {
+        S.hkey[h] = kEmpty;
+        S.hmask[h] = 0u;
+    }
+    for (int i = plo + threadIdx.x; i < phi; i += blockDim.x) {
+        const int rs = (int)(a.pofs[i] - base);
+        const int D = (int)(a.pofs[i + 1] - a.pofs[i]);
+        if (D == 0 || rs >= n) continue;   // a heavy star's row: tg_heavy.cu's
+        const int v = a.vorder[i];
+        for (int k = 0; k < D; k++) {
+            S.vid[rs + k] = v;
+            S.meta[rs + k] = rs | (D << 10);
+        }
+    }
+    cp_async_wait();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) cp_async<16>(&S.tv[e], a.tvs + S.cell[e]);
+    cp_async_commit();
+    cp_async_wait();
+    __syncthreads();
+}
+
 // Fill the (vertex, neighbour) table from the staged cells.  Returns
 // false (block-uniformly) when the table overflows.
-template <typename M>
+// Z: the table's masks were cleared by the staging (stage_rows_a_narrow)
+template <typename M, bool Z>
 __device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vorder, DevStatus *st)
 {
-    for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hmask[h] = 0;
     const int n = S.n;
-    __syncthreads();
+    if constexpr (!Z) {
+        for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hmask[h] = 0;
+        __syncthreads();
+    }
     // insert the 3 other vertices of every staged cell, keyed by the row
     for (int e0 = 0; e0 < n; e0 += blockDim.x) {
         const int e = e0 + threadIdx.x;
@@ -348,7 +391,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
     static_assert(sizeof(S.hkey) >= 4 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
     int *cnt = work + 3 * kCap;
-    if (!stage_cells_and_hash(S, a.vorder, a.st)) return;
+    if (!stage_cells_and_hash<M, sizeof(G) == 4>(S, a.vorder, a.st)) return;
     const int n = S.n;
     for (int e = threadIdx.x; e < n; e += blockDim.x)
         if (m_rs(S.meta[e]) == e) cnt[e] = 0;
@@ -466,7 +509,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<G>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
-    if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.vtp, a.tvs, a.st)) return;
+    if constexpr (sizeof(G) == 4)
+        stage_rows_a_narrow(*reinterpret_cast<Stage<unsigned> *>(raw), a);
+    else if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.vtp, a.tvs, a.st))
+        return;
     G *emask = static_cast<G *>(a.emask);
     if constexpr (sizeof(G) == 8) {
         if (S.wide) {   // block-uniform
