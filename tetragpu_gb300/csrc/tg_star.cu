@@ -98,8 +98,7 @@ struct StageBaseA {
     int meta[kCap];                     // row start | D << 10 | slot of v << 20
     unsigned long long hkey[kHash];     // (row start << 32) | neighbour, kEmpty if free
     short cslot[kCap][3];               // hash slot of each entry's 3 candidates (other vertices)
-    unsigned head[kCap / 32 + 1];       // bit rs: a row starts at entry rs
-    int n, vlo, vhi, full, wide;
+    int n, vlo, vhi, full;
     long long base;
 };
 template <typename M>
@@ -175,7 +174,7 @@ __device__ __forceinline__ unsigned long long hk(int rs, int u)
     return ((unsigned long long)(unsigned)rs << 32) | (unsigned)u;
 }
 
-// Every entry's row: the row starts are marked in a bitmap (head), and an
+// Pass B's rows: the row starts are marked in a bitmap (head), and an
 // entry's row start is the nearest mark at or below it (rows hold at most
 // kMaxStar entries, so the search looks at most three words back).  Only
 // the row starts' vid / meta are written by the rows; the other entries copy
@@ -194,74 +193,15 @@ __device__ __forceinline__ void fill_rows(const unsigned *head, int *vid, int *m
     }
 }
 
-// Stage the block's window: its bounds (the window table's entries, read by
-// every thread), its cells and their sorted vertices (copied asynchronously,
-// issued first), every row's metadata (and whether a star has more than
-// kNarrowStar cells), empty hash keys.  Returns false (block-uniformly) when
-// the window cannot be handled here.  win[b] is the first vertex whose row
-// starts at or after entry kWin * b, wbase[b] that row's first entry.  The
-// cells are staged up to the window's end before heavy rows clip it (at most
-// kCap entries, the most a window of light rows holds).
-__device__ bool stage_rows(StageBaseA &S, const int64_t *__restrict__ pofs,
-                           const int *__restrict__ win, const int *__restrict__ wbase,
-                           const int *__restrict__ vorder, const int *__restrict__ vtp,
-                           const int4 *__restrict__ tvs, DevStatus *st)
-{
-    const int plo = __ldg(win + blockIdx.x), phi = __ldg(win + blockIdx.x + 1);
-    const int base = __ldg(wbase + blockIdx.x);
-    const int nst = min(__ldg(wbase + blockIdx.x + 1) - base, kCap);
-    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<4>(&S.cell[e], vtp + base + e);
-    cp_async_commit();
-    if (threadIdx.x == 0) {
-        S.vlo = plo;
-        S.vhi = phi;
-        S.base = base;
-        S.n = __ldg(wbase + blockIdx.x + 1) - base;
-        S.full = 0;
-        S.wide = 0;
-    }
-    for (int h = threadIdx.x; h < kHash; h += blockDim.x) S.hkey[h] = kEmpty;
-    for (int w = threadIdx.x; w < kCap / 32 + 1; w += blockDim.x) S.head[w] = 0u;
-    __syncthreads();
-    for (int i = plo + threadIdx.x; i < phi; i += blockDim.x) {
-        const int rs = (int)(pofs[i] - base);
-        const int D = (int)(pofs[i + 1] - pofs[i]);
-        if (D == 0) continue;
-        if (D > kMaxStar) {
-            // a heavy row: it and every row after it (heavy too) are
-            // tg_heavy.cu's; the window ends where it starts
-            atomicMin(&S.n, rs);
-            continue;
-        }
-        if (D > kNarrowStar) S.wide = 1;
-        S.vid[rs] = vorder[i];
-        S.meta[rs] = rs | (D << 10);
-        atomicOr(&S.head[rs >> 5], 1u << (rs & 31));
-    }
-    // this thread's cells have landed: gather their vertices
-    cp_async_wait();
-    for (int e = threadIdx.x; e < nst; e += blockDim.x) cp_async<16>(&S.tv[e], tvs + S.cell[e]);
-    cp_async_commit();
-    __syncthreads();
-    const int n = S.n;
-    if (n > kCap) {   // cannot happen: light rows start below kWin and hold <= kMaxStar
-        if (threadIdx.x == 0) {
-            atomicOr(&st->flags, ST_HEAVY_STAR);
-            atomicMin(&st->bad_vertex, vorder[plo]);
-        }
-        return false;
-    }
-    fill_rows(S.head, S.vid, S.meta, n);
-    cp_async_wait();
-    __syncthreads();
-    return true;
-}
-
-// With 32-bit masks in global memory (every window narrow) the staging needs
-// one barrier: the window ends at the next window's first entry or at the
-// first heavy star's (light_end), each row's thread writes its entries' row
-// metadata itself, and the table's keys and masks are cleared here.
-__device__ void stage_rows_a_narrow(Stage<unsigned> &S, const StarA &a)
+// The staging in one barrier: the window ends at the next window's first
+// entry or at the first heavy star's (light_end: heavy stars come after every
+// light one), each row's thread writes its entries' row metadata itself, the
+// table's keys and masks are cleared beside the row loads (as G, the widest
+// masks this launch uses: 64-bit ones cover the 32-bit layout too), and
+// whether a star of the window holds more than kNarrowStar cells (returned,
+// block-uniform) comes from the barrier itself.
+template <typename G>
+__device__ int stage_rows_a1(StageBaseA &S, const StarA &a)
 {
     const int plo = __ldg(a.win + blockIdx.x), phi = __ldg(a.win + blockIdx.x + 1);
     const int base = __ldg(a.wbase + blockIdx.x);
@@ -274,16 +214,18 @@ __device__ void stage_rows_a_narrow(Stage<unsigned> &S, const StarA &a)
         S.base = base;
         S.n = n;
         S.full = 0;
-        S.wide = 0;
     }
+    G *hm = reinterpret_cast<Stage<G> &>(S).hmask;
     for (int h = threadIdx.x; h < kHash; h += blockDim.x) {
         S.hkey[h] = kEmpty;
-        S.hmask[h] = 0u;
+        hm[h] = 0;
     }
+    int wide = 0;
     for (int i = plo + threadIdx.x; i < phi; i += blockDim.x) {
         const int rs = (int)(a.pofs[i] - base);
         const int D = (int)(a.pofs[i + 1] - a.pofs[i]);
         if (D == 0 || rs >= n) continue;   // a heavy star's row: tg_heavy.cu's
+        wide |= D > kNarrowStar;
         const int v = a.vorder[i];
         for (int k = 0; k < D; k++) {
             S.vid[rs + k] = v;
@@ -294,12 +236,12 @@ __device__ void stage_rows_a_narrow(Stage<unsigned> &S, const StarA &a)
     for (int e = threadIdx.x; e < n; e += blockDim.x) cp_async<16>(&S.tv[e], a.tvs + S.cell[e]);
     cp_async_commit();
     cp_async_wait();
-    __syncthreads();
+    return __syncthreads_or(wide);
 }
 
 // Fill the (vertex, neighbour) table from the staged cells.  Returns
 // false (block-uniformly) when the table overflows.
-// Z: the table's masks were cleared by the staging (stage_rows_a_narrow)
+// Z: the table's masks were cleared by the staging (stage_rows_a1)
 template <typename M, bool Z>
 __device__ bool stage_cells_and_hash(Stage<M> &S, const int *__restrict__ vorder, DevStatus *st)
 {
@@ -391,7 +333,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
     static_assert(sizeof(S.hkey) >= 4 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
     int *cnt = work + 3 * kCap;
-    if (!stage_cells_and_hash<M, sizeof(G) == 4>(S, a.vorder, a.st)) return;
+    if (!stage_cells_and_hash<M, true>(S, a.vorder, a.st)) return;
     const int n = S.n;
     for (int e = threadIdx.x; e < n; e += blockDim.x)
         if (m_rs(S.meta[e]) == e) cnt[e] = 0;
@@ -509,13 +451,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<G>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
-    if constexpr (sizeof(G) == 4)
-        stage_rows_a_narrow(*reinterpret_cast<Stage<unsigned> *>(raw), a);
-    else if (!stage_rows(S, a.pofs, a.win, a.wbase, a.vorder, a.vtp, a.tvs, a.st))
-        return;
+    const int wide = stage_rows_a1<G>(S, a);
     G *emask = static_cast<G *>(a.emask);
     if constexpr (sizeof(G) == 8) {
-        if (S.wide) {   // block-uniform
+        if (wide) {   // block-uniform
             star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, emask, n_work);
             return;
         }
