@@ -111,18 +111,18 @@ k_crit_adj(const int64_t *__restrict__ vv_off, const int *__restrict__ vv, int64
     __shared__ int vid[kAdjCap];
     __shared__ int own[kAdjCap];
     __shared__ long long gst[kAdjCap];   // at a row start: the row's first entry in VV
-    __shared__ int s_vlo, s_vhi, s_n, n_own;
-    __shared__ long long s_base;
-    if (threadIdx.x == 0) {
-        s_vlo = win[blockIdx.x];
-        s_vhi = win[blockIdx.x + 1];
-        s_base = ooff[s_vlo];
-        s_n = (int)(ooff[s_vhi] - s_base);
-        n_own = 0;
-    }
-    if (heavy)
+    __shared__ int n_own;
+    // every thread reads the window's bounds itself (the same words: one
+    // transaction each), so the block needs no barrier before the rows
+    // unless the heavy modes mark the slots of rows they leave out
+    const int s_vlo = win[blockIdx.x], s_vhi = win[blockIdx.x + 1];
+    const long long s_base = ooff[s_vlo];
+    const int s_n = (int)(ooff[s_vhi] - s_base);
+    if (threadIdx.x == 0) n_own = 0;
+    if (heavy) {
         for (int e = threadIdx.x; e < kAdjCap; e += blockDim.x) meta[e] = -1;
-    __syncthreads();
+        __syncthreads();
+    }
     const int n = min(s_n, kAdjCap);
     const long long base = s_base;
     if (heavy == 2 && s_n > kAdjCap) {  // a row longer than kMaxDeg lies in this window

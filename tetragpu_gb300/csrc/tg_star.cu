@@ -805,18 +805,10 @@ k_vt_sort(const int64_t *__restrict__ vt_off, const int *__restrict__ win, int *
 {
     griddep_wait();
     __shared__ int cell[kCap], out[kCap], meta[kCap];
-    __shared__ int s_vlo, s_vhi, s_n;
-    __shared__ long long s_base;
-    if (threadIdx.x == 0) {
-        const int vlo = win[blockIdx.x], vhi = win[blockIdx.x + 1];
-        s_vlo = vlo;
-        s_vhi = vhi;
-        s_base = vt_off[vlo];
-        s_n = (int)(vt_off[vhi] - s_base);
-    }
-    __syncthreads();
-    const int n = s_n;
-    const long long base = s_base;
+    // every thread reads the window's bounds itself (the same words)
+    const int s_vlo = win[blockIdx.x], s_vhi = win[blockIdx.x + 1];
+    const long long base = vt_off[s_vlo];
+    const int n = (int)(vt_off[s_vhi] - base);
     if (n > kCap) {
         for (int v = s_vlo + threadIdx.x; v < s_vhi; v += blockDim.x) {
             const int64_t b = vt_off[v], e = vt_off[v + 1];
