@@ -3,7 +3,10 @@ the CPU oracle: each relation's internal inputs (FV and FE read off TF and FT,
 EF off ET and TF, the FF offsets computed with the FF rows, EE from the
 id-sorted incident edges) are made as temporaries when only it is asked for,
 and the result matches the full extraction bit for bit.  A mesh with heavy
-stars takes the slow paths for the same subsets."""
+stars takes the slow paths for the same subsets.  TE, EV, ET, TF, FV, VT and
+VV follow the reference's own CPU code (oracle pinned to its build); FE, FT,
+EF, TT, FF and EE are parity against the restatement (the reference has no
+code for them)."""
 import pytest
 
 from helpers import RELS, assert_relations_equal
