@@ -87,7 +87,12 @@ __device__ __forceinline__ int mpopc(unsigned m) { return __popc(m); }
 __device__ __forceinline__ int mpopc(unsigned long long m) { return __popcll(m); }
 constexpr int kNarrowStar = 32;   // the most cells a star may have for 32-bit masks
 
-constexpr int kRowBoundary = 1 << 30;   // pass A's per-row count word: v has a boundary face
+// pass A's row-start metadata word, above the row start, length and slot
+// fields: the row's neighbour count (bits 22-29; at most 3 * kMaxStar = 192)
+// and whether v has a boundary face (bit 30)
+constexpr int kRowCount = 1 << 22;
+constexpr int kRowBoundary = 1 << 30;
+static_assert(3 * kMaxStar < 256, "the neighbour count must fit its 8 bits");
 
 // Pass A's shared memory: the fields that do not depend on the mask width
 // first (staged before the width is chosen), the masks last.
@@ -329,16 +334,13 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
 {
     // in the hash keys' space once the table is built (only its masks are
     // read after that): the first sightings of owned edges (entry << 2 |
-    // candidate), then per row start the count of neighbours
-    static_assert(sizeof(S.hkey) >= 4 * kCap * sizeof(int), "work list does not fit the keys");
+    // candidate); each row's neighbour count and boundary flag live in the
+    // high bits of its row start's metadata word (kRowCount, kRowBoundary),
+    // zero since the staging wrote it
+    static_assert(sizeof(S.hkey) >= 3 * kCap * sizeof(int), "work list does not fit the keys");
     int *work = reinterpret_cast<int *>(S.hkey);
-    int *cnt = work + 3 * kCap;
     if (!stage_cells_and_hash<M, true>(S, a.vorder, a.st)) return;
     const int n = S.n;
-    for (int e = threadIdx.x; e < n; e += blockDim.x)
-        if (m_rs(S.meta[e]) == e) cnt[e] = 0;
-    if (threadIdx.x == 0) n_work = 0;
-    __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int v = S.vid[e], m = S.meta[e];
         const int rs = m_rs(m), sv = m_sv(m), pos = e - rs;
@@ -353,14 +355,14 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (mctz(cm[k]) != pos) continue;                  // not the first sighting
-            atomicAdd(&cnt[rs], 1);
+            atomicAdd(&S.meta[rs], kRowCount);
             if (get4(w, k + (k >= sv)) > v) work[atomicAdd(&n_work, 1)] = (e << 2) | k;
         }
         // a face at v held by this cell alone (the AND of its two other
         // vertices' masks is this position's bit): v is on the boundary
         const M bit = (M)1 << pos;
         if ((cm[0] & cm[1]) == bit || (cm[0] & cm[2]) == bit || (cm[1] & cm[2]) == bit)
-            atomicOr(&cnt[rs], kRowBoundary);
+            atomicOr(&S.meta[rs], kRowBoundary);
         if (sv <= 1) {
             // faces whose lowest vertex is v: omit slot 1, 2, 3 when v is in
             // slot 0; omit slot 0 when v is in slot 1.  The face's other two
@@ -405,7 +407,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
             const int u = get4(S.tv[e], t);
             mu = S.hmask[S.cslot[e][k]];
             p = 6 * S.cell[e] + pair_slot(sv, t);
-            M mm = (cnt[rs] & kRowBoundary) ? mu : 0;
+            M mm = (S.meta[rs] & kRowBoundary) ? mu : 0;
             if (!mm && sub == 0) n_ef = mpopc(mu);
             for (int q = 0; q < sub; q++) mm &= mm - 1;
             while (mm) {
@@ -431,7 +433,7 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
         const int m = S.meta[e];
         if (m_rs(m) != e) continue;
-        const int d = cnt[e] & ~kRowBoundary;
+        const int d = (m >> 22) & 255;
         a.deg[S.vid[e]] = d;
         // vertices of more than kMaxDeg neighbours take the heavy paths of
         // EE and critical points (tg_heavy.cu); the largest degree tells the
@@ -451,6 +453,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     __shared__ __align__(16) unsigned char raw[sizeof(Stage<G>)];
     __shared__ int n_work;
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
+    if (threadIdx.x == 0) n_work = 0;   // ordered before its use by the staging's barrier
     const int wide = stage_rows_a1<G>(S, a);
     G *emask = static_cast<G *>(a.emask);
     if constexpr (sizeof(G) == 8) {
