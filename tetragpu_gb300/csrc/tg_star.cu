@@ -19,8 +19,9 @@
 // positions whose cell contains it (32-bit in a window whose stars have at
 // most 32 cells, else 64-bit); lanes holding the same key are merged by
 // __match_any_sync first, so one lane per group touches the table.  Pass A
-// leaves every entry's three candidate masks in global memory and pass B
-// stages them instead of rebuilding the table.  With the masks, "first
+// leaves every entry's three candidate masks in global memory (32-bit when no
+// star of the mesh holds more than 32 cells, else 64-bit) and pass B stages
+// them instead of rebuilding the table.  With the masks, "first
 // position holding u" is a count-trailing-zeros and "first position holding
 // x and y" a ctz of an AND.
 //
@@ -40,8 +41,8 @@ namespace {
 
 constexpr int kWin = TG_STAR_WIN;         // VT entries per block window
 constexpr int kCap = kWin + kMaxStar;     // staged entries (rows starting in the window)
-// pass B stages less per entry (no hash), so smaller windows let eight of its
-// blocks share an SM
+// pass B keeps more per entry (neighbour lists, ids, work lists; no table),
+// and its windows are sized so that eight of its blocks share an SM
 constexpr int kWinB = TG_STAR_WIN_B;
 constexpr int kEfLanesA = TG_EFA_LANES;   // lanes per owned edge for its EF count (pass A)
 constexpr int kCapB = kWinB + kMaxStar;
