@@ -44,6 +44,7 @@ CANDIDATES = [
     ("star_b_win_240", {"TG_STAR_WIN_B": 240}),
     ("star_b_win_256", {"TG_STAR_WIN_B": 256}),
     ("star_a_win_192", {"TG_STAR_WIN": 192}),
+    ("efa_lanes_1", {"TG_EFA_LANES": 1}),
     ("ee_group_8", {"TG_EE_GROUP": 8}),
     ("adj_threads_64", {"TG_ADJ_THREADS": 64}),
     ("adj_threads_256", {"TG_ADJ_THREADS": 256}),
