@@ -14,8 +14,8 @@ meshes grouped by tet count, each bucket run as a batch of its own) and on
 the whole batch.  It records every time in tetragpu_gb300/tuning.json
 together with the best setting of each bucket and the setting it selects:
 the one with the smallest total over the buckets, with its margin to each
-bucket's best.  --apply writes the selected defines into csrc/tg_tuning.h,
-which the default build compiles in.
+bucket's best.  --apply merges the selected change into the TUNED block of
+csrc/tg_tuning.h (the settings the default build compiles in).
 
 The batch runs as one disjoint-union mesh, so every kernel launches once per
 batch with one setting; a setting per bucket applies to batches whose
@@ -37,7 +37,8 @@ VARIANTS = os.path.join(PKG, "_build", "variants")
 TUNING_JSON = os.path.join(PKG, "tuning.json")
 TUNING_H = os.path.join(PKG, "csrc", "tg_tuning.h")
 
-# the default setting and one change at a time from it
+# the setting compiled in now ("default": the TUNED block of csrc/tg_tuning.h
+# over the defaults there) and one change at a time from it
 CANDIDATES = [
     ("default", {}),
     ("star_b_win_192", {"TG_STAR_WIN_B": 192}),
@@ -98,6 +99,19 @@ def time_variant(torch, tg, batches, steps: int, warmup: int = 3) -> list:
                 ev[k][1].record(stream)
         torch.cuda.synchronize()
         out.append(sorted(a.elapsed_time(b) for a, b in ev)[steps // 2])   # median
+    return out
+
+
+def tuned_defines(path: str = TUNING_H) -> dict:
+    """The settings the TUNED block of csrc/tg_tuning.h holds now."""
+    with open(path) as fh:
+        text = fh.read()
+    block = text.split("// BEGIN TUNED\n", 1)[1].split("// END TUNED\n", 1)[0]
+    out = {}
+    for line in block.splitlines():
+        parts = line.split()
+        if len(parts) == 3 and parts[0] == "#define":
+            out[parts[1]] = int(parts[2])
     return out
 
 
@@ -162,7 +176,9 @@ def main(argv=None):
         json.dump(rec, fh, indent=1, sort_keys=True)
     print(json.dumps({"selected": selected, "margin_pct": margin, "best": best}))
     if args.apply:
-        write_header(rec["selected_defines"])
+        # every candidate is one change from the settings compiled in now (the
+        # TUNED block; "default" is those settings): keep them, apply the change
+        write_header({**tuned_defines(), **rec["selected_defines"]})
     return rec
 
 
