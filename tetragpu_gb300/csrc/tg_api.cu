@@ -522,13 +522,16 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         tmp.track(vv_off);  // owned by the VV relation once it is ready
         int64_t *deg_sq;  // prefix of deg^2: its total sizes EE (sum deg^2 - 2E)
         TRY(tmp.alloc(&deg_sq, V + 1));
-        // pass A's candidate masks, pass B's input: 32-bit unless a star
-        // holds more than 32 cells
+        // pass A's candidate masks, pass B's input: their low 32 bits for
+        // every entry, the high 32 for the entries of stars of more than 32
+        // cells (an array only when the mesh has such stars; only their
+        // entries of it are touched)
         const bool narrow = !m->wide_stars;
-        uint32_t *emask;
-        TRY(tmp.alloc(&emask, (narrow ? 3 : 6) * NVT));
+        uint32_t *emask, *emask_hi = nullptr;
+        TRY(tmp.alloc(&emask, 3 * NVT));
+        if (!narrow) TRY(tmp.alloc(&emask_hi, 3 * NVT));
         StarA a{m->pofs, m->st_win, m->st_wbase, m->vorder, m->vtp, m->tvs, V, NVT, deg, ecnt,
-                eflag, fflag, fbnd, m->st, emask, narrow, NVT - m->heavy_entries};
+                eflag, fflag, fbnd, m->st, emask, emask_hi, narrow, NVT - m->heavy_entries};
         if (!ecnt) {
             // pass A always records row lengths; give it a throwaway buffer
             TRY(tmp.alloc(&ecnt, 6 * T));
@@ -639,7 +642,7 @@ tg_status run_extract(tg_mesh *m, uint32_t mask, uint32_t opts, cudaStream_t s)
         b.vtp = m->vtp;
         b.tvs = m->tvs; b.V = V; b.nvt = NVT;
         b.vv_off = vv_off; b.erank = erank; b.frank = frank; b.brank = brank;
-        b.emask = emask; b.narrow = narrow; b.vv = vv; b.eid_sorted = eid_sorted;
+        b.emask = emask; b.emask_hi = emask_hi; b.narrow = narrow; b.vv = vv; b.eid_sorted = eid_sorted;
         b.te = te; b.tf = tf; b.ft = ft;
         b.et_off = et_off; b.et = et; b.st = m->st;
         launch_star_b(b, s);

@@ -208,8 +208,11 @@ struct StarA {
     uint32_t *fflag;           // bit per face occurrence 4c+k (first occurrences)
     uint32_t *fbnd;            // bit per face occurrence: first and only (boundary face)
     DevStatus *st;
-    void *emask;               // [3][nvt] star positions holding each entry's candidates
-    bool narrow;               // no star holds more than 32 cells: emask is 32-bit, else 64
+    uint32_t *emask;           // [3][nvt] star positions holding each entry's candidates
+                               // (the low 32 of a star's up to 64 positions)
+    uint32_t *emask_hi;        // [3][nvt] the high 32, written only for stars of more
+                               // than 32 cells; null when the mesh has none
+    bool narrow;               // no star holds more than 32 cells (emask_hi is null)
     int64_t light_end;         // entries of the light stars (they come first): 4T - heavy entries
 };
 void launch_star_a(const StarA &a, cudaStream_t s);
@@ -241,7 +244,8 @@ struct StarB {
     const uint2 *erank;        // {bits, prefix} per 32 edge occurrences
     const uint2 *frank;        // same for face occurrences
     const uint2 *brank;        // same for boundary-face occurrences
-    const void *emask;         // [3][nvt] from pass A
+    const uint32_t *emask;     // [3][nvt] from pass A, as in StarA
+    const uint32_t *emask_hi;
     bool narrow;               // as in StarA
     int32_t *vv;               // [2E] VV rows
     int32_t *eid_sorted;       // [2E] incident edge ids sorted by id, or null

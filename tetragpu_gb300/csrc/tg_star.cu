@@ -19,9 +19,10 @@
 // positions whose cell contains it (32-bit in a window whose stars have at
 // most 32 cells, else 64-bit); lanes holding the same key are merged by
 // __match_any_sync first, so one lane per group touches the table.  Pass A
-// leaves every entry's three candidate masks in global memory (32-bit when no
-// star of the mesh holds more than 32 cells, else 64-bit) and pass B stages
-// them instead of rebuilding the table.  With the masks, "first
+// leaves every entry's three candidate masks in global memory (their low 32
+// bits for every entry, the high 32 in a second array for the entries of
+// stars of more than 32 cells) and pass B stages them instead of rebuilding
+// the table.  With the masks, "first
 // position holding u" is a count-trailing-zeros and "first position holding
 // x and y" a ctz of an AND.
 //
@@ -330,8 +331,8 @@ __device__ __forceinline__ void face_others(const int4 &w, int sv, int o, int &x
 }
 
 // ---------------------------------------------------------------------------
-template <typename M, typename G>
-__device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emask, int &n_work)
+template <typename M>
+__device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, int &n_work)
 {
     // in the hash keys' space once the table is built (only its masks are
     // read after that): the first sightings of owned edges (entry << 2 |
@@ -351,7 +352,9 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             cm[k] = S.hmask[S.cslot[e][k]];
-            emask[k * a.nvt + S.base + e] = (G)cm[k];
+            a.emask[k * a.nvt + S.base + e] = (uint32_t)cm[k];
+            if constexpr (sizeof(M) == 8)
+                if (m_D(m) > kNarrowStar) a.emask_hi[k * a.nvt + S.base + e] = (uint32_t)(cm[k] >> 32);
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -443,8 +446,9 @@ __device__ __forceinline__ void star_a_body(Stage<M> &S, const StarA &a, G *emas
     }
 }
 
-// G: the type the candidate masks are stored as (32-bit when no star of the
-// mesh holds more than kNarrowStar cells, so that no window is wide)
+// G: the widest candidate masks the launch keeps in shared memory (32-bit
+// when no star of the mesh holds more than kNarrowStar cells, so that no
+// window is wide; else 64-bit for the windows holding such a star)
 template <typename G>
 __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 {
@@ -456,14 +460,14 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
     StageBaseA &S = *reinterpret_cast<StageBaseA *>(raw);
     if (threadIdx.x == 0) n_work = 0;   // ordered before its use by the staging's barrier
     const int wide = stage_rows_a1<G>(S, a);
-    G *emask = static_cast<G *>(a.emask);
+
     if constexpr (sizeof(G) == 8) {
         if (wide) {   // block-uniform
-            star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, emask, n_work);
+            star_a_body(*reinterpret_cast<Stage<unsigned long long> *>(raw), a, n_work);
             return;
         }
     }
-    star_a_body(*reinterpret_cast<Stage<unsigned> *>(raw), a, emask, n_work);
+    star_a_body(*reinterpret_cast<Stage<unsigned> *>(raw), a, n_work);
 }
 
 // ---------------------------------------------------------------------------
@@ -473,21 +477,36 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_a(StarA a)
 // as soon as this thread's cells have landed.  Pass A has already rejected
 // every window this cannot hold, so nothing here fails.  Cells are staged up
 // to the window's end before heavy rows clip it (at most kCapB entries).
-// G: the masks' type in global memory; in shared memory they are 32-bit in
-// a window whose stars hold at most kNarrowStar cells (a narrow window of a
-// mesh with 64-bit masks copies their low halves), else 64-bit.
-template <typename M, typename G>
-__device__ __forceinline__ void copy_masks(StageM<M> &S, const StarB &b, const G *emask, int base,
-                                           int nst)
+// The candidate masks into shared memory: 32-bit in a window whose stars
+// hold at most kNarrowStar cells (the low halves), else 64-bit, the high
+// half copied for the entries of stars of more than kNarrowStar cells and
+// zero for the others (which is what their high half is).  The wide form
+// reads each entry's row length, so its rows must be filled in.
+__device__ __forceinline__ void copy_masks(StageM<unsigned> &S, const StarB &b, int base, int nst)
 {
     for (int e = threadIdx.x; e < nst; e += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < 3; k++)   // little-endian: the low half comes first
-            cp_async<sizeof(M)>(&S.cm[e][k], emask + k * b.nvt + base + e);
+        for (int k = 0; k < 3; k++) cp_async<4>(&S.cm[e][k], b.emask + k * b.nvt + base + e);
+}
+__device__ __forceinline__ void copy_masks(StageM<unsigned long long> &S, const StarB &b, int base,
+                                           int nst)
+{
+    for (int e = threadIdx.x; e < nst; e += blockDim.x) {
+        const bool hi = m_D(S.meta[e]) > kNarrowStar;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            unsigned *half = reinterpret_cast<unsigned *>(&S.cm[e][k]);   // little-endian
+            cp_async<4>(half, b.emask + k * b.nvt + base + e);
+            if (hi)
+                cp_async<4>(half + 1, b.emask_hi + k * b.nvt + base + e);
+            else
+                half[1] = 0u;
+        }
+    }
 }
 
 template <typename G>
-__device__ void stage_rows_b(unsigned char *raw, const StarB &b, const G *emask)
+__device__ void stage_rows_b(unsigned char *raw, const StarB &b)
 {
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
     const int plo = __ldg(b.win + blockIdx.x), phi = __ldg(b.win + blockIdx.x + 1);
@@ -527,17 +546,18 @@ __device__ void stage_rows_b(unsigned char *raw, const StarB &b, const G *emask)
     // with 32-bit masks in global memory every window is narrow; else the
     // width is known once the rows are in
     if constexpr (sizeof(G) == 4)
-        copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask, base, nst);
+        copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, base, nst);
     cp_async_commit();
     __syncthreads();
+    fill_rows(S.head, S.vid, S.meta, S.n);
     if constexpr (sizeof(G) == 8) {
+        // each thread's own entries: their rows were filled in just above
         if (S.wide)
-            copy_masks(*reinterpret_cast<StageM<unsigned long long> *>(raw), b, emask, base, nst);
+            copy_masks(*reinterpret_cast<StageM<unsigned long long> *>(raw), b, base, nst);
         else
-            copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, emask, base, nst);
+            copy_masks(*reinterpret_cast<StageM<unsigned> *>(raw), b, base, nst);
         cp_async_commit();
     }
-    fill_rows(S.head, S.vid, S.meta, S.n);
     cp_async_wait();
     __syncthreads();
 }
@@ -760,7 +780,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_star_b(StarB b)
     griddep_wait();
     __shared__ __align__(16) unsigned char raw[sizeof(StageM<G>)];
     StageBaseB &S = *reinterpret_cast<StageBaseB *>(raw);
-    stage_rows_b(raw, b, static_cast<const G *>(b.emask));
+    stage_rows_b<G>(raw, b);
     if constexpr (sizeof(G) == 8) {
         if (S.wide) {   // block-uniform
             star_b_body(*reinterpret_cast<StageM<unsigned long long> *>(raw), b);
